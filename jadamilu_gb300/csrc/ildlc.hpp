@@ -1,0 +1,597 @@
+// Multilevel incomplete LDL^H factorisation with inverse-based pivoting
+// ("ILDLC"), host side.  This is the project's own preconditioner set-up; it
+// plays the role of the reference's ILUPACK chain
+//   symilupackfactor.c:66-221 -> symAMGsetup.c:121-1646 -> sympiluc.F:169
+// (scaling, fill-reducing ordering, Crout ILDL with inverse-based dropping and
+// pivot deferral, 1x1/2x2 pivots, Schur-complement levels, dense last level,
+// SPD conversion of symspd.c:37-1065) without being a port of it:
+//
+//  * scaling is symmetric max-norm equilibration of the current level and is
+//    used only in the decisions (pivot tests, dropping), so the stored factor
+//    needs no row/column scaling vectors at apply time;
+//  * the ordering is a dynamic minimum-degree order on the incomplete
+//    (dropped) pattern, chosen pivot by pivot;
+//  * a pivot k is deferred to the next level when the running estimate of
+//    |e_k^T L^{-1}| exceeds `condest`, or when neither a 1x1 pivot nor a 2x2
+//    pivot with its strongest neighbour keeps the new L entries below
+//    `condest`; deferred rows form the Schur complement of the level;
+//  * the last level accepts every pivot with Bunch-Kaufman 1x1/2x2 choice;
+//  * entries of L are dropped when |l_ik| * |e_k^T L^{-1}| <= droptol
+//    (inverse-based dropping), fill of the Schur complement below droptol/10.
+//
+// All levels are folded into one permuted unit-lower L and a block-diagonal D:
+//   P^T (A - shift I) P  ~=  L D L^H,
+// with the levels recorded as ranges of elimination steps.  The GPU applies
+// the factor by level-scheduled sweeps over L (forward) and L^H (backward).
+#pragma once
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+namespace jdg {
+
+using cplx = std::complex<double>;
+inline double fre(double x) { return x; }
+inline double fre(cplx x) { return x.real(); }
+inline double fcj(double x) { return x; }
+inline cplx fcj(cplx x) { return std::conj(x); }
+inline double fab(double x) { return std::fabs(x); }
+inline double fab(cplx x) { return std::abs(x); }
+
+struct IldlcParams {
+  double droptol = 1e-3;   // inverse-based drop tolerance for L
+  double droptol_schur = -1;  // fill threshold for the Schur complement (<0: droptol/10)
+  double condest = 5.0;    // bound on |e_k^T L^{-1}| (and on scaled L entries)
+  double mem = 20.0;       // max (nnz(L)+n)/nnz(A_upper); <=0: unlimited
+  int max_levels = 12;     // levels before the last (Bunch-Kaufman) level
+  int last_level_min = 64; // a deferred set this small becomes the last level
+  double min_progress = 0.05;  // a level accepting fewer than this fraction ends the recursion
+};
+
+template <class T> struct IldlcFactor {
+  int n = 0;
+  std::vector<int> perm;        // perm[p] = original row (0-based) eliminated at step p
+  std::vector<int64_t> lp;      // CSR of the strictly lower unit L, rows in elimination order
+  std::vector<int> li;          //   column indices (elimination order, < row)
+  std::vector<T> lx;            //   values
+  std::vector<signed char> blk; // 1: 1x1 pivot, 2: first of a 2x2 pivot, -2: second of it
+  std::vector<T> dinv;          // D^{-1}: 1x1 -> 1/d; 2x2 at (p,p+1): diag entries at p and p+1
+  std::vector<T> doff;          // 2x2 D^{-1} off-diagonal (row p, col p+1) stored at p; (p+1,p) = conj
+  std::vector<T> ainv, aoff;    // |D|^{-1} in the same layout (SPD conversion)
+  std::vector<int> level_start; // elimination steps where each level starts, plus n
+  int nneg = 0;                 // negative eigenvalues of D (pivots converted by |D|)
+  int64_t nnz_a_upper = 0;
+  double fill() const { return (double)(li.size() + (size_t)n) / (double)std::max<int64_t>(1, nnz_a_upper); }
+};
+
+namespace detail {
+
+template <class T> struct Ent { int col; T val; };
+
+template <class T> struct Trailing {
+  int n;
+  std::vector<std::vector<Ent<T>>> rows;  // off-diagonal entries of the active matrix (full, Hermitian)
+  std::vector<T> diag;
+};
+
+// bucket queue of nodes keyed by degree
+struct DegQueue {
+  std::vector<int> head, next, prev, key;
+  std::vector<char> in;
+  int minkey = 0, count = 0;
+  void init(int n, int maxkey) {
+    head.assign(maxkey + 2, -1);
+    next.assign(n, -1);
+    prev.assign(n, -1);
+    key.assign(n, 0);
+    in.assign(n, 0);
+    minkey = 0;
+    count = 0;
+  }
+  void grow(int k) {
+    if (k + 2 > (int)head.size()) head.resize(k + 2, -1);
+  }
+  void push(int i, int k) {
+    grow(k);
+    key[i] = k;
+    next[i] = head[k];
+    prev[i] = -1;
+    if (head[k] >= 0) prev[head[k]] = i;
+    head[k] = i;
+    in[i] = 1;
+    if (k < minkey) minkey = k;
+    ++count;
+  }
+  void remove(int i) {
+    if (!in[i]) return;
+    int k = key[i];
+    if (prev[i] >= 0) next[prev[i]] = next[i];
+    else head[k] = next[i];
+    if (next[i] >= 0) prev[next[i]] = prev[i];
+    in[i] = 0;
+    --count;
+  }
+  void update(int i, int k) {
+    if (!in[i] || key[i] == k) return;
+    remove(i);
+    push(i, k);
+  }
+  int pop() {
+    if (count == 0) return -1;
+    while (minkey < (int)head.size() && head[minkey] < 0) ++minkey;
+    int i = head[minkey];
+    remove(i);
+    return i;
+  }
+};
+
+}  // namespace detail
+
+// Factor A - shift*B (B = identity when b == nullptr).  Inputs are the upper
+// triangles in 1-based CSR exactly as the JADAMILU drivers receive them.
+// Returns 0, -1 (bad input), -3 (fill above params.mem), or a positive step
+// number for an exactly zero pivot in the last level.
+template <class T>
+int ildlc_factor(int n, const int* ia, const int* ja, const T* a, double shift, const int* ib, const int* jb,
+                 const T* b, const IldlcParams& prm, IldlcFactor<T>& F) {
+  using namespace detail;
+  if (n <= 0) return -1;
+  Trailing<T> A;
+  A.n = n;
+  A.rows.assign(n, {});
+  A.diag.assign(n, T(0));
+  const int64_t nnzu = (int64_t)ia[n] - ia[0];
+  std::vector<int> cnt(n, 0);
+  for (int i = 0; i < n; ++i)
+    for (int64_t p = ia[i] - 1; p < ia[i + 1] - 1; ++p) {
+      int j = ja[p] - 1;
+      if (j < 0 || j >= n) return -1;
+      if (j != i) { cnt[i]++; cnt[j]++; }
+    }
+  for (int i = 0; i < n; ++i) A.rows[i].reserve(cnt[i] + 8);
+  for (int i = 0; i < n; ++i)
+    for (int64_t p = ia[i] - 1; p < ia[i + 1] - 1; ++p) {
+      int j = ja[p] - 1;
+      T v = a[p];
+      if (j == i) { A.diag[i] += T(fre(v)); continue; }
+      // (i,j) holds A(i,j); row j gets A(j,i) = conj
+      A.rows[i].push_back({j, v});
+      A.rows[j].push_back({i, fcj(v)});
+    }
+  // merge duplicates
+  {
+    std::vector<int> mark(n, -1);
+    for (int i = 0; i < n; ++i) {
+      auto& r = A.rows[i];
+      size_t w = 0;
+      for (size_t q = 0; q < r.size(); ++q) {
+        int c = r[q].col;
+        if (mark[c] >= 0 && mark[c] < (int)w && r[mark[c]].col == c) { r[mark[c]].val += r[q].val; continue; }
+        mark[c] = (int)w;
+        r[w++] = r[q];
+      }
+      r.resize(w);
+      for (auto& e : r) mark[e.col] = -1;
+    }
+  }
+  if (!b)
+    for (int i = 0; i < n; ++i) A.diag[i] -= T(shift);
+  if (b) {
+    for (int i = 0; i < n; ++i)
+      for (int64_t p = ib[i] - 1; p < ib[i + 1] - 1; ++p) {
+        int j = jb[p] - 1;
+        T v = b[p];
+        if (j == i) { A.diag[i] -= T(shift * fre(v)); continue; }
+        T sv = T(-shift) * v;
+        auto upd = [&](int r, int c, T val) {
+          for (auto& e : A.rows[r])
+            if (e.col == c) { e.val += val; return; }
+          A.rows[r].push_back({c, val});
+        };
+        upd(i, j, sv);
+        upd(j, i, fcj(sv));
+      }
+  }
+
+  const double dropS = prm.droptol_schur >= 0 ? prm.droptol_schur : prm.droptol * 0.1;
+  const double kappa = prm.condest;
+  F = IldlcFactor<T>();
+  F.n = n;
+  F.nnz_a_upper = nnzu;
+  std::vector<int> pos(n, -1);          // elimination step of each original row
+  std::vector<int> order;               // original index per step
+  order.reserve(n);
+  std::vector<signed char> blk(n, 0);
+  std::vector<T> dinv(n, T(0)), doff(n, T(0));
+  // L by columns while factoring: for step p, entries (original row i, value)
+  std::vector<int64_t> colptr;
+  colptr.reserve(n + 1);
+  colptr.push_back(0);
+  std::vector<int> crow;
+  std::vector<T> cval;
+  crow.reserve((size_t)nnzu * 3);
+  cval.reserve((size_t)nnzu * 3);
+  const int64_t memcap = prm.mem > 0 ? (int64_t)(prm.mem * (double)nnzu) : INT64_MAX;
+
+  std::vector<char> state(n, 0);  // 0 active candidate, 1 eliminated, 2 deferred
+  std::vector<double> sc(n, 1.0), xi(n, 0.0);
+  std::vector<cplx> xic(n, cplx(0));  // complex estimator accumulators
+  std::vector<int> slot(n, -1);
+  std::vector<int> level_nodes(n);
+  for (int i = 0; i < n; ++i) level_nodes[i] = i;
+  DegQueue Q;
+  int level = 0;
+  bool last = false;
+  std::vector<int> kept;
+  std::vector<T> lk, lj;  // L column values (unscaled) for the pivot(s)
+  std::vector<T> tmpv;
+  const bool is_cplx = !std::is_same<T, double>::value;
+
+  auto remove_col = [&](int r, int c) {
+    auto& row = A.rows[r];
+    for (size_t q = 0; q < row.size(); ++q)
+      if (row[q].col == c) { row[q] = row.back(); row.pop_back(); return; }
+  };
+
+  while (!level_nodes.empty()) {
+    const int nl = (int)level_nodes.size();
+    if (level >= prm.max_levels || nl <= prm.last_level_min) last = true;
+    F.level_start.push_back((int)order.size());
+    // symmetric max-norm scaling of the current level (decisions only)
+    for (int i : level_nodes) {
+      double m = fab(A.diag[i]);
+      for (auto& e : A.rows[i])
+        if (state[e.col] != 1) m = std::max(m, fab(e.val));
+      sc[i] = m > 0 ? 1.0 / std::sqrt(m) : 1.0;
+    }
+    for (int sweep = 0; sweep < 2; ++sweep)
+      for (int i : level_nodes) {
+        double m = fab(A.diag[i]) * sc[i] * sc[i];
+        for (auto& e : A.rows[i]) m = std::max(m, fab(e.val) * sc[i] * sc[e.col]);
+        if (m > 0) sc[i] /= std::sqrt(m);
+      }
+    int maxdeg = 0;
+    for (int i : level_nodes) maxdeg = std::max(maxdeg, (int)A.rows[i].size());
+    Q.init(n, maxdeg + 1);
+    for (int i : level_nodes) {
+      xi[i] = 0;
+      xic[i] = 0;
+      state[i] = 0;
+      Q.push(i, (int)A.rows[i].size());
+    }
+    std::vector<int> deferred;
+    int accepted_here = 0;
+
+    while (Q.count > 0) {
+      int k = Q.pop();
+      if (state[k] != 0) continue;
+      const double sk = sc[k];
+      auto nu_of = [&](int i) { return 1.0 + (is_cplx ? std::abs(xic[i]) : std::fabs(xi[i])); };
+      double nuk = nu_of(k);
+      if (!last && nuk > kappa) { state[k] = 2; deferred.push_back(k); continue; }
+      T dk = A.diag[k];
+      double dks = fab(dk) * sk * sk;
+      // largest scaled entry in column k, and the strongest active neighbour
+      double cmax = 0, amax = 0;
+      int jbest = -1;
+      for (auto& e : A.rows[k]) {
+        double v = fab(e.val) * sk * sc[e.col];
+        cmax = std::max(cmax, v);
+        if (state[e.col] == 0 && v > amax) { amax = v; jbest = e.col; }
+      }
+      int piv = 0;  // 0 defer, 1 one-by-one at k, 2 two-by-two (k, j), 3 one-by-one at jbest
+      if (last) {
+        const double alpha = 0.6404;
+        if (dks > 0 && dks >= alpha * cmax) piv = 1;
+        else if (jbest < 0) piv = dks > 0 ? 1 : -1;
+        else {
+          double sj = sc[jbest], omj = 0;
+          for (auto& e : A.rows[jbest])
+            if (e.col != k) omj = std::max(omj, fab(e.val) * sj * sc[e.col]);
+          double djs = fab(A.diag[jbest]) * sj * sj;
+          if (dks * omj >= alpha * amax * amax) piv = 1;
+          else if (djs >= alpha * omj && djs >= alpha * amax) piv = 3;
+          else piv = 2;
+        }
+        if (piv == -1) {  // structurally and numerically zero row: singular
+          return (int)order.size() + 1;
+        }
+      } else {
+        if (dks > 0 && cmax <= kappa * dks) piv = 1;
+        else if (jbest >= 0 && nu_of(jbest) <= kappa) piv = 2;
+        else piv = 0;
+      }
+      int jp = (piv == 2 || piv == 3) ? jbest : -1;
+      if (piv == 3) {  // pivot on jbest alone; k stays in the queue
+        Q.push(k, (int)A.rows[k].size());
+        k = jp;
+        Q.remove(k);
+        jp = -1;
+        piv = 1;
+        nuk = nu_of(k);
+        dk = A.diag[k];
+      }
+      const double skk = sc[k];
+      if (piv == 1) {
+        // 1x1 pivot at k
+        T d = dk;
+        double nx = last ? 1.0 : nuk;
+        kept.clear();
+        lk.clear();
+        for (auto& e : A.rows[k]) {
+          if (state[e.col] == 1) continue;
+          T l = fcj(e.val) / d;  // L(i,k) = A(i,k)/d, A(i,k) = conj(A(k,i))
+          double ls = fab(l) * sc[e.col] / skk;
+          if (ls * nx <= prm.droptol) continue;
+          kept.push_back(e.col);
+          lk.push_back(l);
+        }
+        // (the row of every neighbour loses column k below)
+        if (!last) {
+          // estimator: choose x_k to maximise growth
+          if (is_cplx) {
+            cplx x = (std::abs(xic[k]) > 0) ? -xic[k] / std::abs(xic[k]) * (1 + std::abs(xic[k])) : cplx(1);
+            for (size_t q = 0; q < kept.size(); ++q) {
+              int i = kept[q];
+              double r = sc[i] / skk;
+              xic[i] += cplx(lk[q] * T(r)) * x;
+            }
+          } else {
+            double x = (xi[k] != 0) ? -(xi[k] / std::fabs(xi[k])) * (1 + std::fabs(xi[k])) : 1.0;
+            for (size_t q = 0; q < kept.size(); ++q) {
+              int i = kept[q];
+              xi[i] += fre(lk[q]) * (sc[i] / skk) * x;
+            }
+          }
+        }
+        // Schur update a_ij -= l_ik d conj(l_jk)
+        for (size_t q = 0; q < kept.size(); ++q) {
+          int i = kept[q];
+          auto& row = A.rows[i];
+          for (size_t t = 0; t < row.size(); ++t) slot[row[t].col] = (int)t;
+          T li = lk[q];
+          A.diag[i] -= T(fre(li * d * fcj(li)));
+          for (size_t t = 0; t < kept.size(); ++t) {
+            if (t == q) continue;
+            int j = kept[t];
+            T u = li * d * fcj(lk[t]);
+            if (slot[j] >= 0) row[slot[j]].val -= u;
+            else if (fab(u) * sc[i] * sc[j] > dropS) { row.push_back({j, -u}); slot[j] = (int)row.size() - 1; }
+          }
+          for (auto& e : row) slot[e.col] = -1;
+        }
+        for (auto& e : A.rows[k]) remove_col(e.col, k);
+        pos[k] = (int)order.size();
+        order.push_back(k);
+        blk[pos[k]] = 1;
+        dinv[pos[k]] = T(1) / d;
+        for (size_t q = 0; q < kept.size(); ++q) { crow.push_back(kept[q]); cval.push_back(lk[q]); }
+        colptr.push_back((int64_t)crow.size());
+        state[k] = 1;
+        A.rows[k].clear();
+        A.rows[k].shrink_to_fit();
+        for (auto& e : kept) (void)e;
+        accepted_here++;
+      } else if (piv == 2) {
+        int j = jp;
+        T akj = T(0);
+        for (auto& e : A.rows[k])
+          if (e.col == j) { akj = e.val; break; }  // A(k,j)
+        T dkk = A.diag[k], djj = A.diag[j];
+        T det = dkk * djj - akj * fcj(akj);
+        double sj = sc[j];
+        double dets = fab(det) * skk * skk * sj * sj, offs = fab(akj) * skk * sj;
+        bool ok = dets > 1e-3 * offs * offs && fab(det) > 0;
+        // gather A(i,k) and A(i,j) for the union of neighbours
+        std::vector<int>& nb = kept;
+        nb.clear();
+        for (auto& e : A.rows[k])
+          if (e.col != j && state[e.col] != 1 && slot[e.col] < 0) { slot[e.col] = (int)nb.size(); nb.push_back(e.col); }
+        for (auto& e : A.rows[j])
+          if (e.col != k && state[e.col] != 1 && slot[e.col] < 0) { slot[e.col] = (int)nb.size(); nb.push_back(e.col); }
+        std::vector<T> aik(nb.size(), T(0)), aij(nb.size(), T(0));
+        for (auto& e : A.rows[k])
+          if (e.col != j && state[e.col] != 1) aik[slot[e.col]] = fcj(e.val);
+        for (auto& e : A.rows[j])
+          if (e.col != k && state[e.col] != 1) aij[slot[e.col]] = fcj(e.val);
+        for (int c : nb) slot[c] = -1;
+        // D^{-1} = (1/det) [djj, -akj; -conj(akj), dkk]
+        T i00 = djj / det, i11 = dkk / det, i01 = -akj / det;  // (k,j) entry
+        T i10 = fcj(i01);
+        lk.assign(nb.size(), T(0));
+        lj.assign(nb.size(), T(0));
+        double lmax = 0;
+        for (size_t q = 0; q < nb.size(); ++q) {
+          lk[q] = aik[q] * i00 + aij[q] * i10;
+          lj[q] = aik[q] * i01 + aij[q] * i11;
+          lmax = std::max(lmax, std::max(fab(lk[q]) * sc[nb[q]] / skk, fab(lj[q]) * sc[nb[q]] / sj));
+        }
+        if (!last && (!ok || lmax > kappa)) {
+          state[k] = 2;
+          deferred.push_back(k);
+          continue;
+        }
+        if (last && !(fab(det) > 0)) return (int)order.size() + 1;
+        double nxk = last ? 1.0 : nu_of(k), nxj = last ? 1.0 : nu_of(j);
+        // dropping per entry
+        std::vector<char> keepk(nb.size()), keepj(nb.size());
+        for (size_t q = 0; q < nb.size(); ++q) {
+          keepk[q] = fab(lk[q]) * sc[nb[q]] / skk * nxk > prm.droptol;
+          keepj[q] = fab(lj[q]) * sc[nb[q]] / sj * nxj > prm.droptol;
+          if (!keepk[q]) lk[q] = T(0);
+          if (!keepj[q]) lj[q] = T(0);
+        }
+        if (!last) {
+          if (is_cplx) {
+            cplx xk = (std::abs(xic[k]) > 0) ? -xic[k] / std::abs(xic[k]) * (1 + std::abs(xic[k])) : cplx(1);
+            cplx xj = (std::abs(xic[j]) > 0) ? -xic[j] / std::abs(xic[j]) * (1 + std::abs(xic[j])) : cplx(1);
+            for (size_t q = 0; q < nb.size(); ++q) {
+              int i = nb[q];
+              xic[i] += cplx(lk[q] * T(sc[i] / skk)) * xk + cplx(lj[q] * T(sc[i] / sj)) * xj;
+            }
+          } else {
+            double xk = (xi[k] != 0) ? -(xi[k] / std::fabs(xi[k])) * (1 + std::fabs(xi[k])) : 1.0;
+            double xj = (xi[j] != 0) ? -(xi[j] / std::fabs(xi[j])) * (1 + std::fabs(xi[j])) : 1.0;
+            for (size_t q = 0; q < nb.size(); ++q) {
+              int i = nb[q];
+              xi[i] += fre(lk[q]) * (sc[i] / skk) * xk + fre(lj[q]) * (sc[i] / sj) * xj;
+            }
+          }
+        }
+        // t_l = D [conj(l_lk); conj(l_lj)] ; update_il = l_ik t_l0 + l_ij t_l1
+        std::vector<int> act;
+        for (size_t q = 0; q < nb.size(); ++q)
+          if (keepk[q] || keepj[q]) act.push_back((int)q);
+        for (int qa : act) {
+          int i = nb[qa];
+          auto& row = A.rows[i];
+          for (size_t t = 0; t < row.size(); ++t) slot[row[t].col] = (int)t;
+          for (int ta : act) {
+            int l = nb[ta];
+            T c0 = fcj(lk[ta]), c1 = fcj(lj[ta]);
+            T t0 = dkk * c0 + akj * c1, t1 = fcj(akj) * c0 + djj * c1;
+            T u = lk[qa] * t0 + lj[qa] * t1;
+            if (l == i) { A.diag[i] -= T(fre(u)); continue; }
+            if (slot[l] >= 0) row[slot[l]].val -= u;
+            else if (fab(u) * sc[i] * sc[l] > dropS) { row.push_back({l, -u}); slot[l] = (int)row.size() - 1; }
+          }
+          for (auto& e : row) slot[e.col] = -1;
+        }
+        for (auto& e : A.rows[k]) if (e.col != j) remove_col(e.col, k);
+        for (auto& e : A.rows[j]) if (e.col != k) remove_col(e.col, j);
+        Q.remove(j);
+        pos[k] = (int)order.size();
+        order.push_back(k);
+        pos[j] = (int)order.size();
+        order.push_back(j);
+        blk[pos[k]] = 2;
+        blk[pos[j]] = -2;
+        dinv[pos[k]] = i00;
+        dinv[pos[j]] = i11;
+        doff[pos[k]] = i01;
+        for (size_t q = 0; q < nb.size(); ++q)
+          if (keepk[q]) { crow.push_back(nb[q]); cval.push_back(lk[q]); }
+        colptr.push_back((int64_t)crow.size());
+        for (size_t q = 0; q < nb.size(); ++q)
+          if (keepj[q]) { crow.push_back(nb[q]); cval.push_back(lj[q]); }
+        colptr.push_back((int64_t)crow.size());
+        state[k] = 1;
+        state[j] = 1;
+        A.rows[k].clear();
+        A.rows[k].shrink_to_fit();
+        A.rows[j].clear();
+        A.rows[j].shrink_to_fit();
+        accepted_here += 2;
+      } else {
+        state[k] = 2;
+        deferred.push_back(k);
+        continue;
+      }
+      if ((int64_t)crow.size() + n > memcap) return -3;
+      // degree updates of the touched rows
+      for (int i : kept)
+        if (state[i] == 0) Q.update(i, (int)A.rows[i].size());
+    }
+    level++;
+    if (deferred.empty()) break;
+    if (!last && (double)accepted_here < prm.min_progress * nl) last = true;
+    level_nodes = deferred;
+  }
+  F.level_start.push_back(n);
+  // convert the column-wise L to CSR rows in elimination order
+  F.perm = order;
+  F.blk = blk;
+  F.dinv = dinv;
+  F.doff = doff;
+  std::vector<int64_t> rc(n + 1, 0);
+  for (int p = 0; p < n; ++p)
+    for (int64_t q = colptr[p]; q < colptr[p + 1]; ++q) rc[pos[crow[q]] + 1]++;
+  for (int p = 0; p < n; ++p) rc[p + 1] += rc[p];
+  F.lp = rc;
+  F.li.assign(rc[n], 0);
+  F.lx.assign(rc[n], T(0));
+  std::vector<int64_t> fillp(rc.begin(), rc.end() - 1);
+  for (int p = 0; p < n; ++p)
+    for (int64_t q = colptr[p]; q < colptr[p + 1]; ++q) {
+      int r = pos[crow[q]];
+      F.li[fillp[r]] = p;
+      F.lx[fillp[r]] = cval[q];
+      fillp[r]++;
+    }
+  // |D|^{-1} (SPD conversion) and the count of negative eigenvalues of D
+  F.ainv.assign(n, T(0));
+  F.aoff.assign(n, T(0));
+  F.nneg = 0;
+  for (int p = 0; p < n; ++p) {
+    if (F.blk[p] == 1) {
+      double v = fre(F.dinv[p]);
+      if (v < 0) F.nneg++;
+      F.ainv[p] = T(std::fabs(v));
+    } else if (F.blk[p] == 2) {
+      // eigen-decomposition of the Hermitian 2x2 inverse block [a b; conj(b) c]
+      double a = fre(F.dinv[p]), c = fre(F.dinv[p + 1]);
+      T bo = F.doff[p];
+      double bb = fab(bo);
+      double mid = 0.5 * (a + c), rad = std::sqrt(0.25 * (a - c) * (a - c) + bb * bb);
+      double l1 = mid + rad, l2 = mid - rad;
+      if (l1 < 0) F.nneg++;
+      if (l2 < 0) F.nneg++;
+      // |M| = M * sign-matrix: |M| = (|l1|+|l2|)/2 I + (|l1|-|l2|)/(2 rad) (M - mid I)
+      double al1 = std::fabs(l1), al2 = std::fabs(l2);
+      if (rad > 0) {
+        double s0 = 0.5 * (al1 + al2), s1 = 0.5 * (al1 - al2) / rad;
+        F.ainv[p] = T(s0 + s1 * (a - mid));
+        F.ainv[p + 1] = T(s0 + s1 * (c - mid));
+        F.aoff[p] = T(s1) * bo;
+      } else {
+        F.ainv[p] = T(al1);
+        F.ainv[p + 1] = T(al1);
+        F.aoff[p] = T(0);
+      }
+    }
+  }
+  return 0;
+}
+
+// Forward and backward level schedules of the unit L of a factor: rows of the
+// same level have no dependency on each other.  fwd_rows lists the rows level
+// by level (fwd_ptr), bwd_rows likewise for L^H.
+template <class T>
+void ildlc_levels(const IldlcFactor<T>& F, std::vector<int>& fwd_ptr, std::vector<int>& fwd_rows,
+                  std::vector<int>& bwd_ptr, std::vector<int>& bwd_rows) {
+  const int n = F.n;
+  std::vector<int> lev(n, 0);
+  int nlev = 0;
+  for (int p = 0; p < n; ++p) {
+    int m = 0;
+    for (int64_t q = F.lp[p]; q < F.lp[p + 1]; ++q) m = std::max(m, lev[F.li[q]] + 1);
+    lev[p] = m;
+    nlev = std::max(nlev, m + 1);
+  }
+  auto bucket = [&](const std::vector<int>& lv, int nl, std::vector<int>& ptr, std::vector<int>& rows) {
+    ptr.assign(nl + 1, 0);
+    for (int p = 0; p < n; ++p) ptr[lv[p] + 1]++;
+    for (int l = 0; l < nl; ++l) ptr[l + 1] += ptr[l];
+    rows.assign(n, 0);
+    std::vector<int> f(ptr.begin(), ptr.end() - 1);
+    for (int p = 0; p < n; ++p) rows[f[lv[p]]++] = p;
+  };
+  bucket(lev, n ? nlev : 0, fwd_ptr, fwd_rows);
+  // backward: column p of L (rows r > p with L(r,p) != 0) must be final first
+  std::vector<int> blev(n, 0);
+  int nb = 0;
+  for (int p = n - 1; p >= 0; --p) {
+    // blev[p] already holds max over dependents via the push below
+    nb = std::max(nb, blev[p] + 1);
+    for (int64_t q = F.lp[p]; q < F.lp[p + 1]; ++q) {
+      int c = F.li[q];
+      blev[c] = std::max(blev[c], blev[p] + 1);
+    }
+  }
+  bucket(blev, n ? nb : 0, bwd_ptr, bwd_rows);
+}
+
+}  // namespace jdg

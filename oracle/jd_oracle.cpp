@@ -1,0 +1,646 @@
+// Test infrastructure only: the CPU oracle of the JADAMILU drop-in.
+//
+// Restates, on the CPU and in plain loops, the reference's driver layer:
+//   PJDRVCOM   src/jd/JDaux.F:5-544    (init, adaptive re-factorisation, dispatch)
+//   PJDINIT    src/jd/JDaux.F:549-1325 (shift choice, factor, retries, SPD conversion)
+//   MATVECA    src/jd/JDaux.F:3397-3418 (upper-stored Hermitian SpMV)
+//   DGLPRECSETUP/DGLPRECSOL src/jd/dglprecsetup.c:11-82, dglprecsol.c:8-26
+//   SYMILUPACKSAVEDIAG src/ilupack/symamgsavediag.c (Gershgorin shift)
+//   dsymamgsol / sdsymamgsol src/ilupack/symilupacksol.c:60-128,
+//     singlesymilupacksol.c:69-144 (preconditioner application; the
+//     ICNTL(5)=1 variant demotes the right-hand side, solves in single
+//     precision and promotes the result)
+// around the JD core of jd_core.hpp.  The multilevel factor itself is the
+// project's host factorisation (jadamilu_gb300/csrc/ildlc.hpp); the oracle
+// applies it with sequential triangular solves.
+//
+// Loaded by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg
+// only.  The GPU library never links or calls it.
+#include <chrono>
+#include <complex>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <stdexcept>
+
+#include "../jadamilu_gb300/csrc/ildlc.hpp"
+#include "jd_core.hpp"
+
+namespace orc {
+
+static double now_s() {
+  using namespace std::chrono;
+  return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+// MATVECA: y = A x, A Hermitian given by one triangle, diagonal first per row.
+template <class T> void matveca(int n, const int* ia, const int* ja, const T* a, const T* x, T* y) {
+  for (int i = 0; i < n; ++i) y[i] = T(0);
+  for (int i = 0; i < n; ++i) {
+    int k = ia[i] - 1;
+    y[i] += a[k] * x[i];
+    for (k = ia[i]; k < ia[i + 1] - 1; ++k) {
+      int j = ja[k] - 1;
+      y[i] += a[k] * x[j];
+      y[j] += cj(a[k]) * x[i];
+    }
+  }
+}
+
+// Application of the factor: x = P (L D L^H)^{-1} P^T b, with |D| when spd.
+template <class T, class S>
+void ildl_apply(const jdg::IldlcFactor<T>& F, bool spd, const T* b, T* x, std::vector<S>& y) {
+  const int n = F.n;
+  y.resize(n);
+  for (int p = 0; p < n; ++p) y[p] = S(b[F.perm[p]]);
+  for (int p = 0; p < n; ++p) {
+    S s = y[p];
+    for (int64_t q = F.lp[p]; q < F.lp[p + 1]; ++q) s -= S(F.lx[q]) * y[F.li[q]];
+    y[p] = s;
+  }
+  const std::vector<T>& di = spd ? F.ainv : F.dinv;
+  const std::vector<T>& dof = spd ? F.aoff : F.doff;
+  for (int p = 0; p < n; ++p) {
+    if (F.blk[p] == 1) {
+      y[p] = S(di[p]) * y[p];
+    } else if (F.blk[p] == 2) {
+      S a0 = y[p], a1 = y[p + 1];
+      S o = S(dof[p]);
+      y[p] = S(di[p]) * a0 + o * a1;
+      y[p + 1] = cj(o) * a0 + S(di[p + 1]) * a1;
+      ++p;
+    }
+  }
+  for (int p = n - 1; p >= 0; --p) {
+    S v = y[p];
+    for (int64_t q = F.lp[p]; q < F.lp[p + 1]; ++q) y[F.li[q]] -= cj(S(F.lx[q])) * v;
+  }
+  for (int p = 0; p < n; ++p) x[F.perm[p]] = T(y[p]);
+}
+
+template <class T> struct LowT;
+template <> struct LowT<double> { using type = float; };
+template <> struct LowT<cplx> { using type = std::complex<float>; };
+
+// SYMILUPACKSAVEDIAG: Gershgorin-type lower bound used as the default shift.
+template <class T> double savediag_shift(int n, const int* ia, const int* ja, const T* a) {
+  std::vector<double> disc(n, 0.0), dg(n, 0.0);
+  int ki = 0;
+  double ti = 0;
+  for (int i = 0; i < n; ++i)
+    for (int j = ia[i]; j < ia[i + 1]; ++j) {
+      int k = ja[j - 1] - 1;
+      if (k == i) {
+        dg[i] = re(a[j - 1]);
+        if (i == 0) ti = re(a[j - 1]);
+        else {
+          if (re(a[j - 1]) < ti) ti = re(a[j - 1]);
+          ki = i;
+        }
+      } else {
+        double v = ab(a[j - 1]);
+        disc[i] += v;
+        disc[k] += v;
+      }
+    }
+  double val = ti - disc[ki];
+  for (int i = 0; i < n; ++i) {
+    double tmp = dg[i] - disc[i];
+    if (tmp < val && dg[i] - ti < disc[ki]) val = tmp;
+  }
+  return val;
+}
+
+// SYMILUPACKSAVEDIAGGEP (symamgsavediaggep.c): the same bound for the pencil,
+// after a symmetric diagonal scaling from B's row sums.
+template <class T>
+double savediag_shift_gep(int n, const int* ia, const int* ja, const T* a, const int* ib, const int* jb, const T* b) {
+  std::vector<double> disc(n, 0.0), dg(n, 0.0);
+  for (int i = 0; i < n; ++i)
+    for (int j = ib[i]; j < ib[i + 1]; ++j)
+      if (jb[j - 1] - 1 == i) dg[i] = re(b[j - 1]);
+  for (int i = 0; i < n; ++i)
+    for (int j = ib[i]; j < ib[i + 1]; ++j) {
+      int k = jb[j - 1] - 1;
+      if (k != i) {
+        double val = std::sqrt(dg[i] / dg[k]);
+        dg[i] += ab(b[j - 1]) * val;
+        dg[k] += ab(b[j - 1]) / val;
+      }
+    }
+  for (int i = 0; i < n; ++i) dg[i] = 1 / std::sqrt(dg[i]);
+  int ki = 0;
+  double ti = 0;
+  for (int i = 0; i < n; ++i)
+    for (int j = ia[i]; j < ia[i + 1]; ++j) {
+      int k = ja[j - 1] - 1;
+      if (k == i) {
+        double val = dg[i] * re(a[j - 1]) * dg[k];
+        if (i == 0) ti = val;
+        else if (val < ti) { ti = val; ki = i; }
+      } else {
+        double val = dg[i] * ab(a[j - 1]) * dg[k];
+        disc[i] += val;
+        disc[k] += val;
+      }
+    }
+  for (int i = 0; i < n; ++i)
+    for (int j = ia[i]; j < ia[i + 1]; ++j)
+      if (ja[j - 1] - 1 == i) dg[i] = dg[i] * re(a[j - 1]) * dg[i];
+  double val = ti - disc[ki];
+  for (int i = 0; i < n; ++i) {
+    double tmp = dg[i] - disc[i];
+    if (tmp < val && dg[i] - ti < disc[ki]) val = tmp;
+  }
+  return val;
+}
+
+struct PrecondFailure {};
+
+// COMMON /PJDINITPJD/ and /ILUPACKMEM/ of the reference, one per precision.
+template <class T> struct Global {
+  double timefact = -1, shift0 = 0, droptol0 = 0, diagmin = 0, shiftmax = 0, memrequested = 0, memused = 0,
+         condest0 = 5;
+  const double slightlyless = 0.8, toldiv = 2.0;
+  int factdgl = 0, factspd = 0, prvdr = 0;
+  bool reenterfirsttime = false, flagsingle = false;
+  jdg::IldlcFactor<T> F;
+  std::vector<double> diag;  // diagonal preconditioner 1/(a_ii - shift)
+  JdShared sh;
+  int nfactor = 0;  // factorisations performed (diagnostic)
+  void cleanup1() {
+    factdgl = 0;
+    F = jdg::IldlcFactor<T>();
+    diag.clear();
+  }
+};
+template <class T> Global<T>& G() {
+  static Global<T> g;
+  return g;
+}
+
+// DGLPRECSETUP (a holds the n diagonal entries)
+template <class T> void dglprecsetup(Global<T>& g, const T* a, int n, int isearch, double shift, double& shift0) {
+  g.diag.assign(n, 0.0);
+  double dmin = re(a[0]), ta = dmin;
+  for (int i = 1; i < n; ++i) {
+    dmin = std::min(dmin, re(a[i]));
+    ta = std::max(ta, re(a[i]));
+  }
+  g.diagmin = dmin;
+  double ati = std::fabs(dmin), ata = std::min(std::fabs(ta), ati);
+  double del = std::max(ta - dmin, ata);
+  if (isearch <= 1) {
+    shift0 = dmin - del / n;
+    g.factspd = -1;
+    if (isearch == 1 && shift < dmin) {
+      shift0 = shift;
+      g.factspd = 0;
+    }
+    for (int i = 0; i < n; ++i) g.diag[i] = 1.0 / (re(a[i]) - shift0);
+  } else {
+    g.factspd = 0;
+    del = 1.0 / del;
+    for (int i = 0; i < n; ++i) {
+      double t = re(a[i]) - shift0;
+      t = (t > 0) ? std::max(t, del) : std::min(t, -del);
+      g.diag[i] = 1.0 / t;
+    }
+  }
+  g.factdgl = 1;
+}
+
+// swap the diagonal entry to the front of each row (JDaux.F:215-229, 1010-1023)
+template <class T> void diag_first(int n, int* ia, int* ja, T* a) {
+  for (int i = 0; i < n; ++i)
+    for (int j = ia[i] - 1; j < ia[i + 1] - 1; ++j)
+      if (ja[j] - 1 == i) {
+        int l = ia[i] - 1;
+        std::swap(ja[j], ja[l]);
+        std::swap(a[j], a[l]);
+      }
+}
+
+// PJDINIT.  Returns ierr (0 ok).
+template <class T>
+int pjdinit(Global<T>& g, int n, T* a, int* ja, int* ia, const T* b, const int* jb, const int* ib, double sigma,
+            int isearch, double& SHIFT, double& DROPTOL, double& MEM, const int* icntl, bool gep) {
+  if (g.factdgl != 0) g.cleanup1();
+  if (ja[0] < 0) {
+    if (isearch >= 2) g.shift0 = sigma;
+    double s0 = g.shift0;
+    dglprecsetup(g, a, n, isearch, SHIFT, s0);
+    g.shift0 = s0;
+    return 0;
+  }
+  if (DROPTOL < 0) DROPTOL = 1e-2;
+  double condest = (g.timefact > 0) ? g.condest0 : (icntl[3] <= 0 ? 5.0 : (double)icntl[3]);
+  if (MEM <= 0) MEM = 10.0;
+  int newsh = 0;
+  for (;;) {
+    double tic = now_s();
+    g.diagmin = 0;
+    for (int i = 0; i < n; ++i) {
+      double val = 0;
+      for (int j = ia[i] - 1; j < ia[i + 1] - 1; ++j)
+        if (ja[j] - 1 == i) val = re(a[j]);
+      g.diagmin = (i == 0) ? val : std::min(val, g.diagmin);
+    }
+    g.shift0 = savediag_shift(n, ia, ja, a);
+    if (gep) g.shift0 = savediag_shift_gep(n, ia, ja, a, ib, jb, b);
+    if (isearch >= 2) g.shift0 = sigma;
+    int ggsh = 0;
+    if (isearch == 1 && SHIFT < g.diagmin) g.shift0 = SHIFT;
+    else ggsh = 1;
+    if (isearch <= 0 && newsh == 1) g.shift0 = SHIFT;
+    if (newsh != 1 && g.timefact <= 0) g.shiftmax = g.diagmin;
+    g.memrequested = MEM;
+    const int recompilu = (icntl[1] == 0 || icntl[1] == -2) ? 1 : -1;
+    const double nposeig = (icntl[2] <= 0) ? 0.01 : 0.0;
+    jdg::IldlcParams prm;
+    prm.droptol = DROPTOL;
+    prm.condest = condest;
+    prm.mem = MEM;
+    int ierr = jdg::ildlc_factor<T>(n, ia, ja, a, g.shift0, gep ? ib : nullptr, gep ? jb : nullptr,
+                                    gep ? b : nullptr, prm, g.F);
+    g.nfactor++;
+    g.memused = (ierr == 0) ? g.F.fill() + 0.05 : MEM;
+    diag_first(n, ia, ja, a);
+    if (ierr == -3 || ierr == -2) {
+      if (!(recompilu == -1 || g.prvdr == -1)) {
+        g.prvdr = 1;
+        DROPTOL = DROPTOL * 2 * g.toldiv;
+        g.cleanup1();
+        continue;
+      }
+    } else if (ierr == -5 || ierr == -6 || ierr > 0) {
+      if (!(recompilu == -1 || g.prvdr == 1) && g.memused < g.slightlyless * g.memrequested) {
+        if (g.memused < (3 * g.slightlyless - 2) * g.memrequested) DROPTOL /= 4 * g.toldiv;
+        else if (g.memused < (2 * g.slightlyless - 1) * g.memrequested) DROPTOL /= 2 * g.toldiv;
+        else DROPTOL /= g.toldiv;
+        DROPTOL = std::max(DROPTOL, 1.01 * std::sqrt(DBL_EPSILON * 0.5));
+        g.prvdr = -1;
+        g.cleanup1();
+        continue;
+      }
+    }
+    if (ierr != 0) {
+      g.cleanup1();
+      return ierr;
+    }
+    double totaltime = now_s() - tic;
+    g.factspd = 0;
+    if (isearch <= 1) {
+      g.factspd = g.F.nneg;
+      if (g.factspd > 0) {
+        if (!(recompilu == -1 || g.factspd <= n * nposeig)) {
+          g.shiftmax = std::min(g.shift0, g.shiftmax);
+          SHIFT = 2 * SHIFT - g.diagmin;
+          newsh = 1;
+          g.prvdr = std::min(g.prvdr, 0);
+          g.cleanup1();
+          continue;
+        }
+      } else if (isearch <= 0 || newsh == 1 || ggsh == 1) {
+        g.factspd = -1;
+      }
+    }
+    g.timefact = std::max(totaltime, 1e-2);
+    g.factdgl = -1;
+    g.droptol0 = DROPTOL;
+    g.condest0 = condest;
+    return 0;
+  }
+}
+
+template <class T> struct PjdCtx {
+  Global<T>* g;
+  int n;
+  T *a, *b;
+  int *ia, *ja, *ib, *jb;
+  bool gep, single;
+  // adaptive re-factorisation inputs
+  int* neig;
+  double* eigs;
+  double* gap;
+  int nw, isearch;
+  const int* icntl;
+  double sigma, tol;
+  double *shift, *droptol, *mem;
+  double tic = 0, rprev = 1;
+  // user matvec (reverse-communication emulation); nullptr: MATVECA
+  void (*user_mv)(void*, int, const T*, T*, T*) = nullptr;
+  void* user_ctx = nullptr;
+  std::vector<typename LowT<T>::type> ylo;
+  std::vector<T> yhi;
+};
+
+template <class T> void pjd_matvec(void* c, int which, const T* x, T* y, T* by) {
+  PjdCtx<T>& C = *(PjdCtx<T>*)c;
+  if (C.user_mv) { C.user_mv(C.user_ctx, which, x, y, by); return; }
+  if (which == 1 || which == 3) matveca(C.n, C.ia, C.ja, C.a, x, y);
+  if ((which == 1 || which == 4) && C.gep) matveca(C.n, C.ib, C.jb, C.b, x, by);
+}
+
+template <class T> void pjd_precond(void* c, const T* rhs, T* sol) {
+  PjdCtx<T>& C = *(PjdCtx<T>*)c;
+  Global<T>& g = *C.g;
+  JdShared& S = g.sh;
+  const double EPSMACH = DBL_EPSILON * 0.5;
+  const int* icntl = C.icntl;
+  const int NEIG = *C.neig, NW = C.nw;
+  double* EIGS = C.eigs;
+  double& SHIFT = *C.shift;
+  double& DROPTOL = *C.droptol;
+  bool reinit = false;
+  int factspd0 = 0;
+  double toc = now_s();
+  auto E = [&](int i) { return EIGS[i - 1]; };
+  if (g.factdgl > 0 && !S.flagcg && C.isearch <= 1 && (icntl[1] == 0 || icntl[1] == -2) && icntl[0] != 2) {
+    double tent;
+    if (NEIG >= 1) { tent = E(NW); factspd0 = -1; }
+    else {
+      tent = S.shift1 - S.rcurr;
+      factspd0 = -1;
+      if (10 * S.rcurr >= g.diagmin - tent && S.shift1 > g.shift0) factspd0 = g.factspd;
+    }
+    if (g.diagmin > tent && factspd0 < 0 && 10 * std::fabs(g.shift0 - tent) >= (g.diagmin - g.shift0)) {
+      SHIFT = tent;
+      reinit = true;
+    }
+  }
+  if (g.factdgl < 0 && !S.flagcg && (icntl[1] == 0 || icntl[1] == -2) && icntl[0] != 2 &&
+      S.rcum - C.rprev <= 6 * std::log(S.rinit / C.tol)) {
+    double tmsol = toc - C.tic, time0, time1;
+    if (tmsol < 1e-1) tmsol = 0;
+    if (S.rcum > C.rprev) {
+      time1 = tmsol * std::log(S.rinit / C.tol) / (S.rcum - C.rprev);
+      time0 = tmsol * std::log(S.rcurr / C.tol) / (S.rcum - C.rprev);
+    } else {
+      time1 = 4 * g.timefact;
+      time0 = 6 * g.timefact;
+    }
+    if (2 * g.timefact < time1 && 4 * g.timefact < time0 + (NW - NEIG - 1) * time1) {
+      if (g.factspd < 0) {
+        double tent, delta;
+        if (NEIG >= 1) {
+          delta = (NEIG > 1) ? std::fabs(E(NW) - E(NW - NEIG + 1)) / (NEIG - 1) : std::max(*C.gap, 0.0);
+          tent = std::min(2 * g.shiftmax - E(NW), E(NW) - delta);
+        } else {
+          tent = std::min(2 * g.shiftmax - S.shift1, S.shift1 - S.rcurr - std::max(*C.gap, 0.0));
+          if (2 * S.rcurr >= g.diagmin - tent) factspd0 = g.factspd;
+        }
+        if ((factspd0 == 0 || 4 * g.timefact < time0) && g.diagmin > tent && 2 * (tent - g.shift0) >= (g.diagmin - g.shift0)) {
+          SHIFT = tent;
+          C.rprev = S.rcum;
+          reinit = true;
+        }
+      }
+      if (factspd0 >= 0 && !reinit && g.memused < g.slightlyless * g.memrequested && g.prvdr <= 0 &&
+          DROPTOL >= std::sqrt(EPSMACH)) {
+        if (icntl[1] != -2) g.reenterfirsttime = false;
+        double DT0 = DROPTOL;
+        if (!g.reenterfirsttime) {
+          if (g.memused < (3 * g.slightlyless - 2) * g.memrequested) DROPTOL /= 4 * g.toldiv;
+          else if (g.memused < (2 * g.slightlyless - 1) * g.memrequested) DROPTOL /= 2 * g.toldiv;
+          else DROPTOL /= g.toldiv;
+          DROPTOL = std::max(DROPTOL, 1.01 * std::sqrt(EPSMACH));
+        }
+        C.rprev = S.rcum;
+        reinit = true;
+        if (DROPTOL == 1.01 * std::sqrt(EPSMACH) && DT0 == DROPTOL && !g.reenterfirsttime) reinit = false;
+        g.reenterfirsttime = false;
+        SHIFT = g.shift0;
+        if (g.factspd > 0) {
+          if (NEIG >= 1) {
+            double delta = (NEIG > 1) ? (E(NW) - E(NW - NEIG + 1)) / (NEIG - 1) : std::max(*C.gap, 0.0);
+            SHIFT = std::min(std::min(2 * g.shift0 - E(NW), E(NW) - delta), g.shiftmax);
+          } else if (g.shift0 > S.shift1) {
+            SHIFT = std::min(S.shift1, g.shiftmax);
+          }
+        }
+      } else if (g.factspd > 0) {
+        if (NEIG >= 1) {
+          if (g.shift0 > E(NW)) {
+            double delta = (NEIG > 1) ? (E(NW) - E(NW - NEIG + 1)) / (NEIG - 1) : std::max(*C.gap, 0.0);
+            SHIFT = std::min(E(NW) - delta, g.shiftmax);
+            C.rprev = S.rcum;
+            reinit = true;
+          }
+        } else if (g.shift0 > S.shift1 && 2 * (g.shift0 - S.shift1) >= (g.diagmin - g.shift0)) {
+          SHIFT = std::min(S.shift1, g.shiftmax);
+          C.rprev = S.rcum;
+          reinit = true;
+        }
+      }
+    }
+  }
+  if (reinit) {
+    int ierr = pjdinit(g, C.n, C.a, C.ja, C.ia, C.b, C.jb, C.ib, C.sigma, std::max(C.isearch, 1), SHIFT, DROPTOL,
+                       *C.mem, icntl, C.gep);
+    if (ierr != 0) {
+      g.factdgl = 1;
+      throw PrecondFailure();
+    }
+    double t = now_s();
+    S.timeilu += std::max(t - toc, 0.0);
+    C.tic = t;
+    if (factspd0 < 0 && g.factspd <= 0) g.factspd = factspd0;
+  }
+  if (g.factdgl > 0) {
+    for (int i = 0; i < C.n; ++i) sol[i] = T(g.diag[i]) * rhs[i];
+  } else if (C.single) {
+    ildl_apply(g.F, C.isearch <= 1, rhs, sol, C.ylo);
+  } else {
+    ildl_apply(g.F, C.isearch <= 1, rhs, sol, C.yhi);
+  }
+}
+
+// PJDRVCOM with the matvec done by MATVECA (or a user callback) and the
+// preconditioner by the factor or the diagonal.
+template <class T>
+void pjd(int n, T* a, int* ja, int* ia, T* b, int* jb, int* ib, double* EIGS, double* RES, T* X, long LX, int& NEIG,
+         double SIGMA, int ISEARCH, int NINIT, int MADSPACE, int& ITER, double TOL, double& SHIFT, double& DROPTOL,
+         double& MEM, int* ICNTL, int& INFO, double& GAP, bool GEP, void (*user_mv)(void*, int, const T*, T*, T*),
+         void* user_ctx) {
+  Global<T>& g = G<T>();
+  JdShared& S = g.sh;
+  g.flagsingle = ICNTL[4] != 0;
+  int ierr = 0;
+  double t0 = now_s();
+  if ((ICNTL[1] != -1 && ICNTL[1] != -2) || g.factdgl == 0) {
+    g.prvdr = 0;
+    g.timefact = -1;
+    g.cleanup1();
+    ierr = pjdinit(g, n, a, ja, ia, b, jb, ib, SIGMA, ISEARCH, SHIFT, DROPTOL, MEM, ICNTL, GEP);
+    g.reenterfirsttime = false;
+  } else {
+    g.prvdr = 0;
+    g.reenterfirsttime = true;
+    S.rinit = S.rcurr = S.rcum = 0;
+    if (ja[0] < 0) {
+      if (ISEARCH >= 2) g.shift0 = SIGMA;
+    } else {
+      for (int i = 0; i < n; ++i) {
+        double val = 0;
+        for (int j = ia[i] - 1; j < ia[i + 1] - 1; ++j)
+          if (ja[j] - 1 == i) val = re(a[j]);
+        g.diagmin = (i == 0) ? val : std::min(val, g.diagmin);
+      }
+      if (!GEP) g.shift0 = savediag_shift(n, ia, ja, a);
+      if (ISEARCH >= 2) g.shift0 = SIGMA;
+      if (ISEARCH == 1 && SHIFT < g.diagmin) g.shift0 = SHIFT;
+      diag_first(n, ia, ja, a);
+      S.timeilu = 0;
+    }
+  }
+  if (ierr != 0) {
+    INFO = -54321;
+    return;
+  }
+  PjdCtx<T> C;
+  C.g = &g;
+  C.n = n;
+  C.a = a; C.b = b; C.ia = ia; C.ja = ja; C.ib = ib; C.jb = jb;
+  C.gep = GEP;
+  C.single = g.flagsingle;
+  C.neig = &NEIG;
+  C.eigs = EIGS;
+  C.gap = &GAP;
+  C.nw = NEIG;
+  C.isearch = ISEARCH;
+  C.icntl = ICNTL;
+  C.sigma = SIGMA;
+  C.tol = TOL;
+  C.shift = &SHIFT;
+  C.droptol = &DROPTOL;
+  C.mem = &MEM;
+  C.tic = now_s();
+  C.rprev = 1.0;
+  C.user_mv = user_mv;
+  C.user_ctx = user_ctx;
+  (void)t0;
+  JdCore<T> core;
+  core.sh = &S;
+  core.cb.matvec = pjd_matvec<T>;
+  core.cb.precond = pjd_precond<T>;
+  core.cb.ctx = &C;
+  try {
+    core.run(n, EIGS, RES, X, LX, NEIG, SIGMA, ISEARCH, NINIT, MADSPACE, ITER, TOL, INFO, GAP, GEP);
+  } catch (PrecondFailure&) {
+    INFO = -54321;
+    return;
+  }
+  // suggested SHIFT / DROPTOL for a restart (JDaux.F:482-535)
+  SHIFT = g.shift0;
+  if (g.factdgl >= 0) {
+    SHIFT = EIGS[0];
+  } else if (g.factspd != 0 || ISEARCH <= 0) {
+    double delta = (NEIG > 1) ? (EIGS[NEIG - 1] - EIGS[0]) / (NEIG - 1) : std::max(GAP, 0.0);
+    if (g.factspd > 0) {
+      SHIFT = std::min(SHIFT, g.shiftmax);
+      SHIFT = std::min(2 * SHIFT - EIGS[0], EIGS[0] - delta);
+    } else {
+      SHIFT = std::min(2 * g.shiftmax - EIGS[0], EIGS[0] - delta);
+      if (g.shift0 < EIGS[0]) SHIFT = std::max(SHIFT, g.shift0);
+    }
+  }
+}
+
+}  // namespace orc
+
+using orc::cplx;
+extern "C" {
+
+typedef void (*orc_dmv_t)(void*, int, const double*, double*, double*);
+typedef void (*orc_dpc_t)(void*, const double*, double*);
+typedef void (*orc_zmv_t)(void*, int, const cplx*, cplx*, cplx*);
+typedef void (*orc_zpc_t)(void*, const cplx*, cplx*);
+
+// DJDREVCOM / DJDREVCOM_GEP semantics with callbacks in place of IJOB returns.
+void orc_djd(int n, double* eigs, double* res, double* x, long lx, int* neig, double sigma, int isearch, int ninit,
+             int madspace, int* iter, double tol, int* info, double* gap, int gep, orc_dmv_t mv, orc_dpc_t pc,
+             void* ctx) {
+  static orc::JdShared sh;
+  orc::JdCore<double> core;
+  core.sh = &sh;
+  core.cb = {mv, pc, ctx};
+  core.run(n, eigs, res, x, lx, *neig, sigma, isearch, ninit, madspace, *iter, tol, *info, *gap, gep != 0);
+}
+void orc_zjd(int n, double* eigs, double* res, cplx* x, long lx, int* neig, double sigma, int isearch, int ninit,
+             int madspace, int* iter, double tol, int* info, double* gap, int gep, orc_zmv_t mv, orc_zpc_t pc,
+             void* ctx) {
+  static orc::JdShared sh;
+  orc::JdCore<cplx> core;
+  core.sh = &sh;
+  core.cb = {mv, pc, ctx};
+  core.run(n, eigs, res, x, lx, *neig, sigma, isearch, ninit, madspace, *iter, tol, *info, *gap, gep != 0);
+}
+
+// DPJD / DPJD_GEP (user_mv == NULL) and DPJDREVCOM (user_mv given).
+void orc_dpjd(int n, double* a, int* ja, int* ia, double* b, int* jb, int* ib, double* eigs, double* res, double* x,
+              long lx, int* neig, double sigma, int isearch, int ninit, int madspace, int* iter, double tol,
+              double* shift, double* droptol, double* mem, int* icntl, int* info, double* gap, int gep,
+              orc_dmv_t user_mv, void* user_ctx) {
+  orc::pjd<double>(n, a, ja, ia, b, jb, ib, eigs, res, x, lx, *neig, sigma, isearch, ninit, madspace, *iter, tol,
+                   *shift, *droptol, *mem, icntl, *info, *gap, gep != 0, user_mv, user_ctx);
+}
+void orc_zpjd(int n, cplx* a, int* ja, int* ia, cplx* b, int* jb, int* ib, double* eigs, double* res, cplx* x,
+              long lx, int* neig, double sigma, int isearch, int ninit, int madspace, int* iter, double tol,
+              double* shift, double* droptol, double* mem, int* icntl, int* info, double* gap, int gep,
+              orc_zmv_t user_mv, void* user_ctx) {
+  orc::pjd<cplx>(n, a, ja, ia, b, jb, ib, eigs, res, x, lx, *neig, sigma, isearch, ninit, madspace, *iter, tol,
+                 *shift, *droptol, *mem, icntl, *info, *gap, gep != 0, user_mv, user_ctx);
+}
+void orc_dpjdcleanup(void) { orc::G<double>().cleanup1(); }
+void orc_zpjdcleanup(void) { orc::G<cplx>().cleanup1(); }
+int orc_nfactor_d(void) { return orc::G<double>().nfactor; }
+
+// MATVECA on its own (kernel parity).
+void orc_dmatveca(int n, const int* ia, const int* ja, const double* a, const double* x, double* y) {
+  orc::matveca(n, ia, ja, a, x, y);
+}
+void orc_zmatveca(int n, const int* ia, const int* ja, const cplx* a, const cplx* x, cplx* y) {
+  orc::matveca(n, ia, ja, a, x, y);
+}
+
+// Factor (the project's host code) + the oracle's application of it, on an
+// opaque handle, for kernel-level parity of the GPU preconditioner.
+struct OrcFactorD { jdg::IldlcFactor<double> F; };
+void* orc_dfactor(int n, const int* ia, const int* ja, const double* a, double shift, double droptol, double condest,
+                  double mem, int* ierr) {
+  auto* h = new OrcFactorD;
+  jdg::IldlcParams p;
+  p.droptol = droptol;
+  p.condest = condest;
+  p.mem = mem;
+  *ierr = jdg::ildlc_factor<double>(n, ia, ja, a, shift, nullptr, nullptr, nullptr, p, h->F);
+  return h;
+}
+void orc_dfactor_info(void* h, long* out) {
+  auto& F = ((OrcFactorD*)h)->F;
+  std::vector<int> fp, fr, bp, br;
+  jdg::ildlc_levels(F, fp, fr, bp, br);
+  out[0] = F.n;
+  out[1] = (long)F.li.size();
+  out[2] = F.nneg;
+  out[3] = (long)F.level_start.size() - 1;
+  out[4] = (long)fp.size() - 1;
+  out[5] = (long)bp.size() - 1;
+  long n2 = 0;
+  for (int p = 0; p < F.n; ++p) n2 += F.blk[p] == 2;
+  out[6] = n2;
+}
+void orc_dfactor_apply(void* h, int spd, int single, const double* b, double* x) {
+  auto& F = ((OrcFactorD*)h)->F;
+  if (single) {
+    std::vector<float> y;
+    orc::ildl_apply(F, spd != 0, b, x, y);
+  } else {
+    std::vector<double> y;
+    orc::ildl_apply(F, spd != 0, b, x, y);
+  }
+}
+void orc_dfactor_free(void* h) { delete (OrcFactorD*)h; }
+
+}  // extern "C"
