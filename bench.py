@@ -1,0 +1,364 @@
+"""Benchmark: seconds to 10 interior eigenpairs of the 3-D Anderson model.
+
+Workload: Anderson model on a 100^3 periodic lattice (n = 1e6, hopping -1,
+diagonal i.i.d. uniform in [-8.25, 8.25] from a seeded splitmix64 stream),
+10 eigenpairs closest to sigma = 0, residual tolerance 1e-10, float64
+Jacobi-Davidson with the multilevel ILDL preconditioner stored and applied in
+float32 (ICNTL(5)=1).  Synthetic data generated in-process.
+
+A step is one complete solve (DPJD with NINIT=0) to 10 converged eigenpairs.
+The preconditioner is factored once on the host before the timed region
+(reported as ``factor_s``) and reused with ICNTL(2) = -1, the reference's
+static-reuse mode; every timed step runs the whole eigensolve.
+
+``value``: seconds per solve with the matrix resident in HBM (CUDA events on
+the solver stream).  ``e2e``: the same through the Fortran-style C ABI
+(dpjd_) with host arrays: matrix upload, solve and eigenvector download.
+``roofline``: the preconditioner application (the dominant kernels).
+``cpu_baseline``: the CPU oracle (a restatement of the reference's algorithm)
+timed on a bounded number of iterations of the same workload with the same
+factor, scaled by the GPU solve's MATVEC count.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+Multi-GPU runs are independent replicas (the single-matrix path does not
+shard); rank 0 prints the line.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "s to 10 eigpairs at resid 1e-10 (3D Anderson 100^3, sigma=0, FP32 factor / FP64 outer)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--size", type=int, default=100, help="lattice edge (100: n = 1e6, the benchmark workload)")
+    ap.add_argument("--droptol", type=float, default=3e-3)
+    ap.add_argument("--mem", type=float, default=60.0)
+    ap.add_argument("--precision", type=int, default=1, help="ICNTL(5): 0 fp64, 1 fp32, 2 bf16 factor")
+    ap.add_argument("--neig", type=int, default=10)
+    ap.add_argument("--cpu-seconds", type=float, default=20.0, help="budget of the CPU-baseline sample")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Clocks:
+    """Samples SM clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def workload(size):
+    from jadamilu_gb300 import matrices as M
+    ia, ja, a = M.anderson3d(size, disorder=16.5, seed=0)
+    return ia, ja, a
+
+
+def solve_kwargs(args, icntl2):
+    return dict(isearch=2, sigma=0.0, madspace=25, maxit=100000, tol=1e-10, droptol=args.droptol, mem=args.mem,
+                icntl=(0, icntl2, 0, 0, args.precision))
+
+
+def cpu_baseline_sample(J, ia, ja, a, args, gpu_iter):
+    """Oracle iterations on the same matrix with the GPU run's factor."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib
+    L = J.load()
+    n_out = np.zeros(1, np.int32)
+    nnz = np.zeros(1, np.int64)
+    sh = np.zeros(1)
+    p = lambda v: v.ctypes.data_as(C.c_void_p)
+    L.jdgpu_dfactor_export.argtypes = [C.c_void_p] * 12
+    L.jdgpu_dfactor_export(p(n_out), p(nnz), p(sh), *([None] * 9))
+    n, nz = int(n_out[0]), int(nnz[0])
+    perm = np.zeros(n, np.int32)
+    lp = np.zeros(n + 1, np.int64)
+    li = np.zeros(nz, np.int32)
+    lx = np.zeros(nz)
+    blk = np.zeros(n, np.int8)
+    dinv, doff, ainv, aoff = (np.zeros(n) for _ in range(4))
+    L.jdgpu_dfactor_export(p(n_out), p(nnz), p(sh), p(perm), p(lp), p(li), p(lx), p(blk), p(dinv), p(doff),
+                           p(ainv), p(aoff))
+    O = oracle_lib.lib()
+    O.orc_dimport_factor.argtypes = [C.c_int] + [C.c_void_p] * 9 + [C.c_double]
+    O.orc_dimport_factor(n, p(perm), p(lp), p(li), p(lx), p(blk), p(dinv), p(doff), p(ainv), p(aoff), float(sh[0]))
+    # bounded sample: a capped number of MATVECs; grow the cap until it runs long enough
+    cap, dt, it = 8, 0.0, 0
+    while True:
+        kw = solve_kwargs(args, -1)
+        kw["maxit"] = cap
+        t0 = time.perf_counter()
+        r = oracle_lib.dpjd(ia, ja, a, args.neig, **kw)
+        dt = time.perf_counter() - t0
+        it = r["iter"]
+        if dt * 2 > args.cpu_seconds or cap >= gpu_iter:
+            break
+        cap = min(gpu_iter, int(cap * max(2.0, args.cpu_seconds / max(dt, 1e-3) * 0.6)))
+    per_mv = dt / max(it, 1)
+    return {"value": per_mv * gpu_iter, "unit": "s", "cores": 1, "kind": "port",
+            "sample": f"CPU oracle, same matrix and factor, {it} MATVECs in {dt:.1f} s "
+                      f"({per_mv * 1e3:.1f} ms/MATVEC) scaled to the GPU solve's {gpu_iter} MATVECs"}
+
+
+def run_gb300(args):
+    rank, world, local = dist_env()
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", init_method="env://")
+    import jadamilu_gb300 as J
+    from jadamilu_gb300 import build
+    build.build_all()
+    L = J.load()
+    ia, ja, a = workload(args.size)
+    n = len(ia) - 1
+    nnz_upper = len(a)
+    stream = torch.cuda.Stream()
+    J.set_stream(stream.cuda_stream)
+    J.prepare_matrix((a, ja, ia))
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # factorisation (host) + first solve; then warm-up solves reusing the factor
+    J.reset_stats()
+    t0 = time.perf_counter()
+    r = J.dpjd((a, ja, ia), args.neig, **solve_kwargs(args, 1))
+    first_s = time.perf_counter() - t0
+    st = J.stats()
+    if r["info"] != 0:
+        raise SystemExit(f"first solve failed: INFO={r['info']}")
+    for _ in range(max(0, args.warmup - 1)):
+        r = J.dpjd((a, ja, ia), args.neig, **solve_kwargs(args, -1))
+    # timed region: device-resident solves
+    clocks = Clocks(local)
+    barrier()
+    clocks.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    l0 = L.jdgpu_launch_count()
+    iters, results = [], []
+    e0.record(stream)
+    for _ in range(args.steps):
+        r = J.dpjd((a, ja, ia), args.neig, **solve_kwargs(args, -1))
+        iters.append(r["iter"])
+        results.append(r)
+    e1.record(stream)
+    barrier()
+    ms = e0.elapsed_time(e1) / args.steps
+    launches = L.jdgpu_launch_count() - l0
+    clk = clocks.stop()
+    ms_t = torch.tensor([ms], device="cuda")
+    if world > 1:
+        import torch.distributed as dist
+        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
+    ms = float(ms_t.item())
+    ok = all(rr["info"] == 0 and rr["neig"] == args.neig and np.all(rr["res"] <= 1e-10) for rr in results)
+    eigs = np.sort(results[-1]["eigs"])
+    # roofline of the dominant kernels (preconditioner application) and of SpMV
+    pb = np.zeros(5)
+    L.jdgpu_dprecond_bench.argtypes = [C.c_int, C.c_void_p]
+    L.jdgpu_dprecond_bench(20, pb.ctypes.data_as(C.c_void_p))
+    sb = np.zeros(4)
+    L.jdgpu_dspmv_bench.argtypes = [C.c_int, C.c_void_p]
+    L.jdgpu_dspmv_bench(50, sb.ctypes.data_as(C.c_void_p))
+    peak, peak_kind = measured_peaks()
+    prec_gbs = pb[1] / (pb[0] * 1e-3) / 1e9
+    spmv_gbs = sb[1] / (sb[0] * 1e-3) / 1e9
+    # e2e: through dpjd_ with host buffers (matrix upload + eigenvector download)
+    J.release_matrix()
+    torch.cuda.synchronize()
+    h2d = (n + 1) * 4 + nnz_upper * 4 + nnz_upper * 8
+    d2h = args.neig * n * 8 + 2 * args.neig * 8
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        re = J.dpjd((a, ja, ia), args.neig, **solve_kwargs(args, -1))
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        try:
+            cpu = cpu_baseline_sample(J, ia, ja, a, args, int(np.median(iters)))
+        except Exception as ex:  # reported, not fatal
+            cpu = {"value": None, "unit": "s", "cores": 1, "kind": "port", "sample": f"failed: {ex}"}
+    if rank == 0:
+        line = {
+            "metric": METRIC,
+            "value": ms / 1e3,
+            "unit": "s",
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": ms,
+            "higher_is_better": False,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f64 outer / f32 factor" if args.precision == 1 else ("f64" if args.precision == 0 else
+                                                                             "f64 outer / bf16 factor"),
+            "data": "synthetic (seeded splitmix64 Anderson disorder)",
+            "config": {"workload": f"anderson3d {args.size}^3 periodic, W=16.5, seed 0, n={n}, "
+                                   f"{args.neig} eigpairs closest to 0, TOL 1e-10",
+                       "n": n, "nnz_upper": nnz_upper, "droptol": args.droptol, "condest": 5.0,
+                       "madspace": 25, "icntl": [0, -1, 0, 0, args.precision],
+                       "factor_s": st["factor_s"], "first_solve_with_factor_s": first_s,
+                       "fill": st["fill"], "nnz_l": st["nnz_l"], "levels": st["levels"],
+                       "fwd_depth": st["fwd_depth"], "matvec_per_solve": int(np.median(iters)),
+                       "parallelism": f"replicas x{world}", "l2": "working set > L2 (no flush needed)",
+                       "eigs_min_max": [float(eigs[0]), float(eigs[-1])], "converged": ok},
+            "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "roofline": {"kernel": "ildl_apply (level-scheduled L, D, L^H sweeps, fp32)", "bound": "hbm",
+                         "achieved": prec_gbs, "peak": peak, "unit": "GB/s", "frac": prec_gbs / peak,
+                         "traffic": None, "bytes_per_launch": pb[1], "ms_per_launch": pb[0],
+                         "peak_kind": peak_kind},
+            "roofline_spmv": {"achieved": spmv_gbs, "peak": peak, "unit": "GB/s", "frac": spmv_gbs / peak,
+                              "bytes_per_launch": sb[1], "ms_per_launch": sb[0]},
+            "gpu_launches": int(launches),
+            "clocks": clk,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def run_reference(args):
+    """The reference path on the host cores: the CPU oracle (the reference's
+    algorithm restated; the Fortran library cannot be built on this image)."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib
+    from jadamilu_gb300 import build
+    build.build_oracle()
+    ia, ja, a = workload(args.size)
+    n = len(ia) - 1
+    O = oracle_lib.lib()
+    # factor once (host), then bounded iteration samples with the static preconditioner
+    t0 = time.perf_counter()
+    kw = solve_kwargs(args, 1)
+    kw["maxit"] = 4
+    oracle_lib.dpjd(ia, ja, a, args.neig, **kw)
+    factor_s = time.perf_counter() - t0
+    per_mv = []
+    cap = 8
+    for step in range(args.warmup + args.steps):
+        kw = solve_kwargs(args, -1)
+        kw["maxit"] = cap
+        t0 = time.perf_counter()
+        r = oracle_lib.dpjd(ia, ja, a, args.neig, **kw)
+        dt = time.perf_counter() - t0
+        if step >= args.warmup:
+            per_mv.append(dt / max(1, r["iter"]))
+        if dt < args.cpu_seconds / 4:
+            cap *= 2
+    # MATVECs to 10 eigenpairs: the oracle runs the same algorithm as the GPU
+    # library; the count for this workload and factor is measured by the GPU
+    # arm (matvec_per_solve) and is passed here when known
+    mv = int(os.environ.get("JDG_MATVEC_PER_SOLVE", "0")) or None
+    v = float(np.median(per_mv)) * (mv if mv else 1)
+    line = {"impl": "reference", "metric": METRIC if mv else METRIC + " [per MATVEC]", "value": v,
+            "unit": "s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64 outer / f32 factor",
+            "data": "synthetic (seeded splitmix64 Anderson disorder)",
+            "config": {"workload": f"anderson3d {args.size}^3 periodic, W=16.5, seed 0, n={n}",
+                       "factor_s": factor_s, "s_per_matvec": float(np.median(per_mv))},
+            "cpu_baseline": {"value": v, "unit": "s", "cores": 1, "kind": "port",
+                             "sample": f"CPU oracle, capped MATVEC samples (up to {cap}) on the full workload"},
+            "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,167 @@
+/*
+ * jadamilu_gb300.h -- C ABI of the GB300 Jacobi-Davidson library.
+ *
+ * The driver entry points are drop-in replacements for the JADAMILU
+ * Fortran drivers: same symbol names (gfortran decoration: lower case plus
+ * a trailing underscore), every argument by reference, 1-based indices,
+ * the same argument lists, ICNTL/IPRINT/INFO meaning and reverse-
+ * communication protocol.  Each declaration cites the reference routine it
+ * replaces; the C prototypes of the reference are in
+ * src/include/jadamilu1.h:22-118 and the Fortran argument documentation in
+ * src/jd/PJD.F and Doc/DPJD_prototypes.f.
+ *
+ * Integers are 32-bit (the reference's default INTEGER).  Complex arrays are
+ * interleaved (re, im) doubles, i.e. COMPLEX*16.
+ *
+ * Extensions beyond the reference:
+ *   ICNTL(5) = 2 stores the preconditioner in bfloat16 (float32 arithmetic);
+ *   jdgpu_* entry points expose single kernels for testing and set options.
+ */
+#ifndef JADAMILU_GB300_H
+#define JADAMILU_GB300_H
+
+#ifdef __cplusplus
+#include <complex>
+typedef std::complex<double> jdg_zcomplex;
+#define JDG_API __attribute__((visibility("default")))
+extern "C" {
+#else
+typedef struct { double re, im; } jdg_zcomplex;
+#define JDG_API
+#endif
+
+/* DPJD: replaces PJD_EV (src/jd/PJD.F:5-262) for real symmetric A.
+ * Built-in matvec and built-in multilevel ILDL preconditioner. */
+JDG_API void dpjd_(int* N, double* A, int* JA, int* IA, double* EIGS, double* RES, double* X, int* LX, int* NEIG,
+                   double* SIGMA, int* ISEARCH, int* NINIT, int* MADSPACE, int* ITER, double* TOL, double* SHIFT,
+                   double* DROPTOL, double* MEM, int* ICNTL, int* IPRINT, int* INFO, double* GAP);
+
+/* DPJDREVCOM: replaces PJDREVCOM_EV (src/jd/PJD.F:268-362).  Returns with
+ * IJOB=1 for X(NDX2) = A*X(NDX1); IJOB=0 when done. */
+JDG_API void dpjdrevcom_(int* N, double* A, int* JA, int* IA, double* EIGS, double* RES, double* X, int* LX,
+                         int* NEIG, double* SIGMA, int* ISEARCH, int* NINIT, int* MADSPACE, int* ITER, double* TOL,
+                         double* SHIFT, double* DROPTOL, double* MEM, int* ICNTL, int* IJOB, int* NDX1, int* NDX2,
+                         int* IPRINT, int* INFO, double* GAP);
+
+/* DJDREVCOM: replaces JDREVCOM_EV (src/jd/PJD.F:369-429).  IJOB=1: matvec
+ * X(NDX2) = A*X(NDX1); IJOB=2: preconditioner solve Prec*X(NDX1) = X(NDX2). */
+JDG_API void djdrevcom_(int* N, double* EIGS, double* RES, double* X, int* LX, int* NEIG, double* SIGMA, int* ISEARCH,
+                        int* NINIT, int* MADSPACE, int* ITER, double* TOL, int* IJOB, int* NDX1, int* NDX2,
+                        int* IPRINT, int* INFO, double* GAP);
+
+/* DPJD_GEP: replaces PJD_GEP (src/jd/PJD.F:492-572), A x = lambda B x, B SPD. */
+JDG_API void dpjd_gep_(int* N, double* A, int* JA, int* IA, double* B, int* JB, int* IB, double* EIGS, double* RES,
+                       double* X, int* LX, int* NEIG, double* SIGMA, int* ISEARCH, int* NINIT, int* MADSPACE,
+                       int* ITER, double* TOL, double* SHIFT, double* DROPTOL, double* MEM, int* ICNTL, int* IPRINT,
+                       int* INFO, double* GAP);
+
+/* DPJDREVCOM_GEP: replaces PJDREVCOM_GEP (src/jd/PJD.F:576-705).  IJOB=1:
+ * X(NDX2)=A*X(NDX1) and X(NDX3)=B*X(NDX1); 3: A only; 4: B only. */
+JDG_API void dpjdrevcom_gep_(int* N, double* A, int* JA, int* IA, double* B, int* JB, int* IB, double* EIGS,
+                             double* RES, double* X, int* LX, int* NEIG, double* SIGMA, int* ISEARCH, int* NINIT,
+                             int* MADSPACE, int* ITER, double* TOL, double* SHIFT, double* DROPTOL, double* MEM,
+                             int* ICNTL, int* IJOB, int* NDX1, int* NDX2, int* NDX3, int* IPRINT, int* INFO,
+                             double* GAP);
+
+/* DJDREVCOM_GEP: replaces JDREVCOM_GEP (src/jd/PJD.F:709-798). */
+JDG_API void djdrevcom_gep_(int* N, double* EIGS, double* RES, double* X, int* LX, int* NEIG, double* SIGMA,
+                            int* ISEARCH, int* NINIT, int* MADSPACE, int* ITER, double* TOL, int* IJOB, int* NDX1,
+                            int* NDX2, int* NDX3, int* IPRINT, int* INFO, double* GAP);
+
+/* DPJDCLEANUP: replaces PJDCLEANUP_EV (src/jd/PJD.F:435-488). */
+JDG_API void dpjdcleanup_(void);
+
+/* Complex Hermitian versions (ZPJD & co.), same argument meaning with
+ * COMPLEX*16 A, B and X (reference C prototypes jadamilu1.h:68-118). */
+JDG_API void zpjd_(int* N, jdg_zcomplex* A, int* JA, int* IA, double* EIGS, double* RES, jdg_zcomplex* X, int* LX,
+                   int* NEIG, double* SIGMA, int* ISEARCH, int* NINIT, int* MADSPACE, int* ITER, double* TOL,
+                   double* SHIFT, double* DROPTOL, double* MEM, int* ICNTL, int* IPRINT, int* INFO, double* GAP);
+JDG_API void zpjdrevcom_(int* N, jdg_zcomplex* A, int* JA, int* IA, double* EIGS, double* RES, jdg_zcomplex* X,
+                         int* LX, int* NEIG, double* SIGMA, int* ISEARCH, int* NINIT, int* MADSPACE, int* ITER,
+                         double* TOL, double* SHIFT, double* DROPTOL, double* MEM, int* ICNTL, int* IJOB, int* NDX1,
+                         int* NDX2, int* IPRINT, int* INFO, double* GAP);
+JDG_API void zjdrevcom_(int* N, double* EIGS, double* RES, jdg_zcomplex* X, int* LX, int* NEIG, double* SIGMA,
+                        int* ISEARCH, int* NINIT, int* MADSPACE, int* ITER, double* TOL, int* IJOB, int* NDX1,
+                        int* NDX2, int* IPRINT, int* INFO, double* GAP);
+JDG_API void zpjd_gep_(int* N, jdg_zcomplex* A, int* JA, int* IA, jdg_zcomplex* B, int* JB, int* IB, double* EIGS,
+                       double* RES, jdg_zcomplex* X, int* LX, int* NEIG, double* SIGMA, int* ISEARCH, int* NINIT,
+                       int* MADSPACE, int* ITER, double* TOL, double* SHIFT, double* DROPTOL, double* MEM, int* ICNTL,
+                       int* IPRINT, int* INFO, double* GAP);
+JDG_API void zpjdrevcom_gep_(int* N, jdg_zcomplex* A, int* JA, int* IA, jdg_zcomplex* B, int* JB, int* IB,
+                             double* EIGS, double* RES, jdg_zcomplex* X, int* LX, int* NEIG, double* SIGMA,
+                             int* ISEARCH, int* NINIT, int* MADSPACE, int* ITER, double* TOL, double* SHIFT,
+                             double* DROPTOL, double* MEM, int* ICNTL, int* IJOB, int* NDX1, int* NDX2, int* NDX3,
+                             int* IPRINT, int* INFO, double* GAP);
+JDG_API void zjdrevcom_gep_(int* N, double* EIGS, double* RES, jdg_zcomplex* X, int* LX, int* NEIG, double* SIGMA,
+                            int* ISEARCH, int* NINIT, int* MADSPACE, int* ITER, double* TOL, int* IJOB, int* NDX1,
+                            int* NDX2, int* NDX3, int* IPRINT, int* INFO, double* GAP);
+JDG_API void zpjdcleanup_(void);
+
+/* ---- single-kernel entry points (host arrays in and out) ---- */
+
+/* Number of visible CUDA devices (0 without a GPU). */
+JDG_API int jdgpu_device_count(void);
+
+/* y = A x on the GPU for A stored like DPJD's A/JA/IA; replaces one call of
+ * MATVECA (src/jd/JDaux.F:3397-3418).  Returns 0 or -1 on a CUDA error. */
+JDG_API int jdgpu_dspmv(int n, const int* ia, const int* ja, const double* a, const double* x, double* y);
+JDG_API int jdgpu_zspmv(int n, const int* ia, const int* ja, const jdg_zcomplex* a, const jdg_zcomplex* x,
+                        jdg_zcomplex* y);
+
+/* Factor A - shift*I with the host ILDLC and apply it on the GPU to nrhs
+ * right-hand sides; replaces SYMILUPACKFACTOR + SYMILUPACKSOL /
+ * SINGLESYMILUPACKSOL (src/ilupack/symilupacksol.c:60-128,
+ * singlesymilupacksol.c:69-104).  spd != 0 applies |D| (SYMSPDCONVERT).
+ * precision: 0 float64, 1 float32 (ICNTL(5)=1), 2 bfloat16 storage.
+ * info (5 entries, may be NULL): nnz(L), negative pivots, levels, forward
+ * and backward schedule depth.  Returns 0, a factorisation error code, or
+ * -99 on a CUDA error. */
+JDG_API int jdgpu_dildl_apply(int n, const int* ia, const int* ja, const double* a, double shift, double droptol,
+                              double condest, int spd, int precision, int nrhs, const double* b, double* x,
+                              long* info);
+
+/* Time `reps` GPU applications of the factor of A - shift*I (inputs resident
+ * on the device, CUDA events).  out (8): ms per application, nnz(L),
+ * forward depth, backward depth, launches per application, factor seconds,
+ * rows solved by the single-CTA tail kernels, unused. */
+JDG_API int jdgpu_dildl_bench(int n, const int* ia, const int* ja, const double* a, double shift, double droptol,
+                              double condest, int spd, int precision, int reps, double* out);
+
+/* Device-resident mode (no reference counterpart; used for repeated solves
+ * and timing): upload A once, let dpjd_ reuse it and keep eigenvectors on the
+ * device, until jdgpu_drelease_matrix(). */
+JDG_API int jdgpu_dprepare_matrix(int n, const int* ia, const int* ja, const double* a);
+JDG_API void jdgpu_drelease_matrix(void);
+JDG_API void jdgpu_dmatrix_info(long* out);
+
+/* Run on the caller's CUDA stream (a cudaStream_t); NULL: the library's own. */
+JDG_API void jdgpu_set_stream(void* stream);
+
+/* Kernels launched by the library so far (graph replays count their nodes). */
+JDG_API long long jdgpu_launch_count(void);
+
+/* Timing of the last real solve's preconditioner / resident SpMV on the
+ * solver stream (no reference counterpart; measurement only).  See
+ * driver.cu for the algorithmic byte counts written to out. */
+JDG_API int jdgpu_dprecond_bench(int reps, double* out);
+JDG_API int jdgpu_dspmv_bench(int reps, double* out);
+
+/* Copy out the host factor of the last real solve (CPU comparison runs). */
+JDG_API int jdgpu_dfactor_export(int* n_out, long long* nnz_out, double* shift_out, int* perm, long long* lp, int* li,
+                                 double* lx, signed char* blk, double* dinv, double* doff, double* ainv,
+                                 double* aoff);
+
+/* Options: "depth_weight" (ordering key weight of the triangular-solve
+ * depth, default 2), "verbose". */
+JDG_API void jdgpu_set_option(const char* name, double value);
+
+/* Statistics of the last real solve (10 doubles): factor seconds, upload
+ * seconds, preconditioner applications, matvecs, levels, forward depth,
+ * backward depth, nnz(L), fill, factorisations. */
+JDG_API void jdgpu_dstats(double* out);
+JDG_API void jdgpu_reset_stats(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

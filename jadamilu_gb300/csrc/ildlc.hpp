@@ -49,6 +49,7 @@ struct IldlcParams {
   int max_levels = 12;     // levels before the last (Bunch-Kaufman) level
   int last_level_min = 64; // a deferred set this small becomes the last level
   double min_progress = 0.05;  // a level accepting fewer than this fraction ends the recursion
+  double depth_weight = 64.0;  // ordering key = degree + depth_weight * (forward level of the row)
 };
 
 template <class T> struct IldlcFactor {
@@ -79,11 +80,12 @@ template <class T> struct Trailing {
 
 // bucket queue of nodes keyed by degree
 struct DegQueue {
-  std::vector<int> head, next, prev, key;
+  std::vector<int> head, tail, next, prev, key;
   std::vector<char> in;
   int minkey = 0, count = 0;
   void init(int n, int maxkey) {
     head.assign(maxkey + 2, -1);
+    tail.assign(maxkey + 2, -1);
     next.assign(n, -1);
     prev.assign(n, -1);
     key.assign(n, 0);
@@ -92,15 +94,19 @@ struct DegQueue {
     count = 0;
   }
   void grow(int k) {
-    if (k + 2 > (int)head.size()) head.resize(k + 2, -1);
+    if (k + 2 > (int)head.size()) {
+      head.resize(k + 2, -1);
+      tail.resize(k + 2, -1);
+    }
   }
-  void push(int i, int k) {
+  void push(int i, int k) {  // FIFO within a bucket
     grow(k);
     key[i] = k;
-    next[i] = head[k];
-    prev[i] = -1;
-    if (head[k] >= 0) prev[head[k]] = i;
-    head[k] = i;
+    prev[i] = tail[k];
+    next[i] = -1;
+    if (tail[k] >= 0) next[tail[k]] = i;
+    else head[k] = i;
+    tail[k] = i;
     in[i] = 1;
     if (k < minkey) minkey = k;
     ++count;
@@ -111,6 +117,7 @@ struct DegQueue {
     if (prev[i] >= 0) next[prev[i]] = next[i];
     else head[k] = next[i];
     if (next[i] >= 0) prev[next[i]] = prev[i];
+    else tail[k] = prev[i];
     in[i] = 0;
     --count;
   }
@@ -220,6 +227,8 @@ int ildlc_factor(int n, const int* ia, const int* ja, const T* a, double shift, 
   std::vector<double> sc(n, 1.0), xi(n, 0.0);
   std::vector<cplx> xic(n, cplx(0));  // complex estimator accumulators
   std::vector<int> slot(n, -1);
+  std::vector<int> dlev(n, 0);  // forward level row i would get if eliminated now
+  auto qkey = [&](int i) { return (int)A.rows[i].size() + (int)(prm.depth_weight * dlev[i]); };
   std::vector<int> level_nodes(n);
   for (int i = 0; i < n; ++i) level_nodes[i] = i;
   DegQueue Q;
@@ -260,7 +269,7 @@ int ildlc_factor(int n, const int* ia, const int* ja, const T* a, double shift, 
       xi[i] = 0;
       xic[i] = 0;
       state[i] = 0;
-      Q.push(i, (int)A.rows[i].size());
+      Q.push(i, qkey(i));
     }
     std::vector<int> deferred;
     int accepted_here = 0;
@@ -306,7 +315,7 @@ int ildlc_factor(int n, const int* ia, const int* ja, const T* a, double shift, 
       }
       int jp = (piv == 2 || piv == 3) ? jbest : -1;
       if (piv == 3) {  // pivot on jbest alone; k stays in the queue
-        Q.push(k, (int)A.rows[k].size());
+        Q.push(k, qkey(k));
         k = jp;
         Q.remove(k);
         jp = -1;
@@ -363,6 +372,7 @@ int ildlc_factor(int n, const int* ia, const int* ja, const T* a, double shift, 
           }
           for (auto& e : row) slot[e.col] = -1;
         }
+        for (int i : kept) dlev[i] = std::max(dlev[i], dlev[k] + 1);
         for (auto& e : A.rows[k]) remove_col(e.col, k);
         pos[k] = (int)order.size();
         order.push_back(k);
@@ -460,6 +470,11 @@ int ildlc_factor(int n, const int* ia, const int* ja, const T* a, double shift, 
           }
           for (auto& e : row) slot[e.col] = -1;
         }
+        {
+          int lv = std::max(dlev[k], dlev[j]) + 1;
+          for (size_t q = 0; q < nb.size(); ++q)
+            if (keepk[q] || keepj[q]) dlev[nb[q]] = std::max(dlev[nb[q]], lv);
+        }
         for (auto& e : A.rows[k]) if (e.col != j) remove_col(e.col, k);
         for (auto& e : A.rows[j]) if (e.col != k) remove_col(e.col, j);
         Q.remove(j);
@@ -493,7 +508,7 @@ int ildlc_factor(int n, const int* ia, const int* ja, const T* a, double shift, 
       if ((int64_t)crow.size() + n > memcap) return -3;
       // degree updates of the touched rows
       for (int i : kept)
-        if (state[i] == 0) Q.update(i, (int)A.rows[i].size());
+        if (state[i] == 0) Q.update(i, qkey(i));
     }
     level++;
     if (deferred.empty()) break;

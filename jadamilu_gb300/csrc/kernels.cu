@@ -1,0 +1,491 @@
+// sm_103a kernels of the Jacobi-Davidson hot path.
+//
+// All of them are HBM-bandwidth kernels (no tensor-core work exists on this
+// path): SpMV over the full Hermitian matrix in SELL-32 layout (coalesced
+// column/value loads), the level-scheduled sweeps of the multilevel LDL^H
+// preconditioner, and the BLAS-1/2 vector work of the outer and inner JD
+// iterations (deterministic two-pass reductions, so results do not depend on
+// the launch).
+#include <atomic>
+
+#include "kernels.cuh"
+
+namespace jdg {
+namespace k {
+
+static std::atomic<long long> g_launches{0};
+long long launch_count() { return g_launches.load(); }
+void add_launches(long long n) { g_launches += n; }
+#define COUNT_LAUNCH() (g_launches += 1)
+
+constexpr int TPB = 256;
+static inline int nblk(long n, int tpb = TPB) { return (int)std::max<long>(1, (n + tpb - 1) / tpb); }
+
+// ---------------------------------------------------------------- SpMV ----
+template <class T>
+__global__ void __launch_bounds__(TPB) spmv_sell_kernel(int n, const int64_t* __restrict__ sptr,
+                                                        const int* __restrict__ col, const T* __restrict__ val,
+                                                        const T* __restrict__ x, T* __restrict__ y) {
+  int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  int sl = r >> 5, lane = r & 31;
+  int64_t b = sptr[sl], e = sptr[sl + 1];
+  T acc = T(0);
+  for (int64_t q = b + lane; q < e; q += 32) acc = fma_(val[q], x[__ldg(col + q)], acc);
+  y[r] = acc;
+}
+template <class T> void spmv(const SellMatrix<T>& A, const T* x, T* y, cudaStream_t s) {
+  spmv_sell_kernel<T><<<nblk(A.n), TPB, 0, s>>>(A.n, A.sptr, A.col, A.val, x, y);
+  COUNT_LAUNCH();
+}
+
+// -------------------------------------------------------------- BLAS-1 ----
+template <class T> __global__ void axpy_kernel(long n, T a, const T* __restrict__ x, T* __restrict__ y) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    y[i] = fma_(a, x[i], y[i]);
+}
+template <class T> __global__ void scal_kernel(long n, double a, T* x) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) x[i] = a * x[i];
+}
+template <class T> __global__ void fill_kernel(long n, T v, T* x) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) x[i] = v;
+}
+static inline int grid_1d(long n) { return (int)std::min<long>(nblk(n), 152L * 16); }
+template <class T> void axpy(long n, T a, const T* x, T* y, cudaStream_t s) {
+  if (n > 0) { axpy_kernel<T><<<grid_1d(n), TPB, 0, s>>>(n, a, x, y); COUNT_LAUNCH(); }
+}
+template <class T> void scal(long n, double a, T* x, cudaStream_t s) {
+  if (n > 0) { scal_kernel<T><<<grid_1d(n), TPB, 0, s>>>(n, a, x); COUNT_LAUNCH(); }
+}
+template <class T> void fill(long n, T v, T* x, cudaStream_t s) {
+  if (n > 0) { fill_kernel<T><<<grid_1d(n), TPB, 0, s>>>(n, v, x); COUNT_LAUNCH(); }
+}
+
+// ---------------------------------------------------- reductions (V^H w) ----
+__device__ __forceinline__ double shfl_down(double v, int o) { return __shfl_down_sync(0xffffffffu, v, o); }
+__device__ __forceinline__ zc shfl_down(zc v, int o) { return zc(shfl_down(v.x, o), shfl_down(v.y, o)); }
+__device__ __forceinline__ float shfl_xor_any(float v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
+__device__ __forceinline__ double shfl_xor_any(double v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
+__device__ __forceinline__ cc shfl_xor_any(cc v, int o) { return cc(shfl_xor_any(v.x, o), shfl_xor_any(v.y, o)); }
+__device__ __forceinline__ zc shfl_xor_any(zc v, int o) { return zc(shfl_xor_any(v.x, o), shfl_xor_any(v.y, o)); }
+
+constexpr int MD_CH = 8;  // columns per pass
+static inline int md_grid(long n) { return (int)std::min<long>(std::max<long>(1, (n + 2047) / 2048), 152L * 4); }
+long mdot_partial_size(long n, int k) { return (long)md_grid(n) * ((k + MD_CH - 1) / MD_CH) * MD_CH; }
+
+template <class T>
+__global__ void __launch_bounds__(TPB) mdot_partial_kernel(long n, int k, const T* __restrict__ V, long ldv,
+                                                           const T* __restrict__ w, T* __restrict__ partial) {
+  const int c0 = blockIdx.y * MD_CH;
+  const int nc = min(MD_CH, k - c0);
+  T acc[MD_CH];
+#pragma unroll
+  for (int j = 0; j < MD_CH; ++j) acc[j] = T(0);
+  for (long i = blockIdx.x * (long)TPB + threadIdx.x; i < n; i += (long)gridDim.x * TPB) {
+    T wi = w[i];
+#pragma unroll
+    for (int j = 0; j < MD_CH; ++j)
+      if (j < nc) acc[j] = fma_(cj(V[i + (long)(c0 + j) * ldv]), wi, acc[j]);
+  }
+  __shared__ T red[TPB / 32][MD_CH];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int j = 0; j < MD_CH; ++j) {
+    T v = acc[j];
+    for (int o = 16; o > 0; o >>= 1) v += shfl_down(v, o);
+    if (lane == 0) red[wid][j] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < MD_CH) {
+    T v = T(0);
+    for (int q = 0; q < TPB / 32; ++q) v += red[q][threadIdx.x];
+    partial[(long)(c0 + threadIdx.x) * gridDim.x + blockIdx.x] = v;
+  }
+}
+template <class T>
+__global__ void __launch_bounds__(TPB) mdot_final_kernel(int g, const T* __restrict__ partial, T* __restrict__ out) {
+  const int c = blockIdx.x;
+  T v = T(0);
+  for (int q = threadIdx.x; q < g; q += TPB) v += partial[(long)c * g + q];
+  __shared__ T red[TPB / 32];
+  for (int o = 16; o > 0; o >>= 1) v += shfl_down(v, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    T t = T(0);
+    for (int q = 0; q < TPB / 32; ++q) t += red[q];
+    out[c] = t;
+  }
+}
+template <class T> void mdot(long n, int k, const T* V, long ldv, const T* w, T* out, T* partial, cudaStream_t s) {
+  if (k <= 0) return;
+  int g = md_grid(n);
+  dim3 grid(g, (k + MD_CH - 1) / MD_CH);
+  mdot_partial_kernel<T><<<grid, TPB, 0, s>>>(n, k, V, ldv, w, partial);
+  mdot_final_kernel<T><<<k, TPB, 0, s>>>(g, partial, out);
+  g_launches += 2;
+}
+
+// ------------------------------------------------------ V y (tall-skinny) ----
+constexpr int GMV_MAX = 64;
+template <class T> struct SmallVec { T v[GMV_MAX]; };
+
+template <class T>
+__global__ void __launch_bounds__(TPB) gemv_dev_kernel(long n, int k, T alpha, const T* __restrict__ V, long ldv,
+                                                       const T* __restrict__ y, T beta, T* __restrict__ w) {
+  __shared__ T ys[GMV_MAX];
+  if (threadIdx.x < k) ys[threadIdx.x] = y[threadIdx.x];
+  __syncthreads();
+  for (long i = blockIdx.x * (long)TPB + threadIdx.x; i < n; i += (long)gridDim.x * TPB) {
+    T acc = T(0);
+    for (int c = 0; c < k; ++c) acc = fma_(V[i + (long)c * ldv], ys[c], acc);
+    T o = (beta == T(0)) ? T(0) : beta * w[i];
+    w[i] = fma_(alpha, acc, o);
+  }
+}
+template <class T>
+__global__ void __launch_bounds__(TPB) gemv_val_kernel(long n, int k, T alpha, const T* __restrict__ V, long ldv,
+                                                       SmallVec<T> y, T beta, T* __restrict__ w) {
+  for (long i = blockIdx.x * (long)TPB + threadIdx.x; i < n; i += (long)gridDim.x * TPB) {
+    T acc = T(0);
+    for (int c = 0; c < k; ++c) acc = fma_(V[i + (long)c * ldv], y.v[c], acc);
+    T o = (beta == T(0)) ? T(0) : beta * w[i];
+    w[i] = fma_(alpha, acc, o);
+  }
+}
+template <class T>
+void gemv_dev(long n, int k, T alpha, const T* V, long ldv, const T* y, T beta, T* w, cudaStream_t s) {
+  if (k > GMV_MAX) throw std::runtime_error("gemv_dev: too many columns");
+  if (k <= 0) {
+    if (!(beta == T(1))) {
+      if (beta == T(0)) fill(n, T(0), w, s);
+      else throw std::runtime_error("gemv_dev: unsupported beta");
+    }
+    return;
+  }
+  gemv_dev_kernel<T><<<grid_1d(n), TPB, 0, s>>>(n, k, alpha, V, ldv, y, beta, w);
+  COUNT_LAUNCH();
+}
+template <class T>
+void gemv_val(long n, int k, T alpha, const T* V, long ldv, const T* yh, T beta, T* w, cudaStream_t s) {
+  if (k > GMV_MAX) throw std::runtime_error("gemv_val: too many columns");
+  if (k <= 0) {
+    if (beta == T(0)) fill(n, T(0), w, s);
+    return;
+  }
+  SmallVec<T> y;
+  for (int c = 0; c < k; ++c) y.v[c] = yh[c];
+  gemv_val_kernel<T><<<grid_1d(n), TPB, 0, s>>>(n, k, alpha, V, ldv, y, beta, w);
+  COUNT_LAUNCH();
+}
+
+template <class T> struct SmallMat { T q[32 * 32]; };
+template <class T>
+__global__ void __launch_bounds__(TPB) rmult_kernel(long n, int K, int keep, const T* __restrict__ V, long ldv,
+                                                    const T* __restrict__ Q, T* __restrict__ out) {
+  __shared__ T qs[32 * 32];
+  for (int t = threadIdx.x; t < K * keep; t += TPB) qs[t] = Q[t];
+  __syncthreads();
+  for (long i = blockIdx.x * (long)TPB + threadIdx.x; i < n; i += (long)gridDim.x * TPB) {
+    T row[32];
+    for (int kk = 0; kk < K; ++kk) row[kk] = V[i + (long)kk * ldv];
+    for (int c = 0; c < keep; ++c) {
+      T acc = T(0);
+      for (int kk = 0; kk < K; ++kk) acc = fma_(row[kk], qs[kk + c * K], acc);
+      out[i + (long)c * n] = acc;
+    }
+  }
+}
+template <class T> void rmult(long n, int K, int keep, const T* V, long ldv, const T* Qh, T* out, cudaStream_t s) {
+  if (K > 32) throw std::runtime_error("rmult: search space above 32");
+  // Q travels through a small device staging area owned by the kernel launch
+  static thread_local T* dq = nullptr;
+  if (!dq) CK(cudaMalloc(&dq, sizeof(T) * 32 * 32));
+  std::vector<T> q(K * keep);
+  for (int c = 0; c < keep; ++c)
+    for (int kk = 0; kk < K; ++kk) q[kk + c * K] = Qh[kk + c * K];
+  CK(cudaMemcpyAsync(dq, q.data(), sizeof(T) * K * keep, cudaMemcpyHostToDevice, s));
+  CK(cudaStreamSynchronize(s));  // the pageable source must not change before the copy
+  rmult_kernel<T><<<grid_1d(n), TPB, 0, s>>>(n, K, keep, V, ldv, dq, out);
+  COUNT_LAUNCH();
+}
+
+template <class T> __global__ void diag_kernel(long n, const double* __restrict__ d, const T* __restrict__ r, T* x) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    x[i] = d[i] * r[i];
+}
+template <class T> void diagsolve(long n, const double* d, const T* rhs, T* sol, cudaStream_t s) {
+  diag_kernel<T><<<grid_1d(n), TPB, 0, s>>>(n, d, rhs, sol);
+  COUNT_LAUNCH();
+}
+
+// ------------------------------------------------ multilevel LDL^H apply ----
+template <class T, class A>
+__global__ void ildl_gather_kernel(int n, const int* __restrict__ orig, const T* __restrict__ b, A* __restrict__ y) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < n) y[s] = cvt<A>(b[orig[s]]);
+}
+template <class T, class A>
+__global__ void ildl_scatter_kernel(int n, const int* __restrict__ orig, const A* __restrict__ y, T* __restrict__ x) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < n) x[orig[s]] = cvt<T>(y[s]);
+}
+template <class S, class A>
+__global__ void ildl_dsolve_kernel(int n, const signed char* __restrict__ blk, const int* __restrict__ partner,
+                                   const S* __restrict__ dv, const S* __restrict__ dof, A* __restrict__ y) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  signed char b = blk[s];
+  if (b == 1) {
+    y[s] = ld_arith(dv + s) * y[s];
+  } else if (b == 2) {
+    int t = partner[s];
+    A a0 = y[s], a1 = y[t], o = ld_arith(dof + s);
+    y[s] = fma_(ld_arith(dv + s), a0, o * a1);
+    y[t] = fma_(cj(o), a0, ld_arith(dv + t) * a1);
+  }
+}
+// A run of narrow levels [l0, l1) in one CTA: a warp per row, levels
+// separated by __syncthreads (which orders the CTA's global writes).
+__device__ __forceinline__ float wsum(float v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double wsum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ cc wsum(cc v) { return cc(wsum(v.x), wsum(v.y)); }
+__device__ __forceinline__ zc wsum(zc v) { return zc(wsum(v.x), wsum(v.y)); }
+
+constexpr int RUN_TPB = 1024;
+template <class S, class A>
+__global__ void __launch_bounds__(RUN_TPB) ildl_run_kernel(int l0, int l1, const int* __restrict__ lptr,
+                                                          const int* __restrict__ rows, const int64_t* __restrict__ rp,
+                                                          const int* __restrict__ ci, const S* __restrict__ cv,
+                                                          A* y) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int l = l0; l < l1; ++l) {
+    const int lo = lptr[l], hi = lptr[l + 1];
+    for (int t = lo + warp; t < hi; t += RUN_TPB / 32) {
+      const int s = rows ? rows[t] : t;
+      const int64_t b = rp[s], e = rp[s + 1];
+      A acc = A(0);
+      for (int64_t q = b + lane; q < e; q += 32) acc = fma_(ld_arith(cv + q), y[ci[q]], acc);
+      acc = wsum(acc);
+      if (lane == 0) y[s] = y[s] - acc;
+    }
+    __syncthreads();
+  }
+}
+// One wide level: 8 lanes per row.
+constexpr int WIDE_TPB = 256, WIDE_LANES = 8;
+template <class S, class A>
+__global__ void __launch_bounds__(WIDE_TPB) ildl_wide_kernel(int lo, int hi, const int* __restrict__ rows,
+                                                            const int64_t* __restrict__ rp, const int* __restrict__ ci,
+                                                            const S* __restrict__ cv, A* __restrict__ y) {
+  const int g = blockIdx.x * (WIDE_TPB / WIDE_LANES) + (threadIdx.x / WIDE_LANES);
+  const int lane = threadIdx.x % WIDE_LANES;
+  const int t = lo + g;
+  const bool ok = t < hi;
+  int s = 0;
+  A acc = A(0);
+  if (ok) {
+    s = rows ? rows[t] : t;
+    const int64_t b = rp[s], e = rp[s + 1];
+    for (int64_t q = b + lane; q < e; q += WIDE_LANES) acc = fma_(ld_arith(cv + q), y[ci[q]], acc);
+  }
+  for (int o = WIDE_LANES / 2; o > 0; o >>= 1) acc = acc + shfl_xor_any(acc, o);
+  if (ok && lane == 0) y[s] = y[s] - acc;
+}
+
+// Forward tail, external part: y[s] -= sum over entries with column < s_tail.
+template <class S, class A>
+__global__ void __launch_bounds__(WIDE_TPB) tail_ext_kernel(int m, int s_tail, const int64_t* __restrict__ rp,
+                                                           const int* __restrict__ ci, const S* __restrict__ cv,
+                                                           A* __restrict__ y) {
+  const int t = blockIdx.x * (WIDE_TPB / WIDE_LANES) + (threadIdx.x / WIDE_LANES);
+  const int lane = threadIdx.x % WIDE_LANES;
+  A acc = A(0);
+  if (t < m)
+    for (int64_t q = rp[t] + lane; q < rp[t + 1]; q += WIDE_LANES) acc = fma_(ld_arith(cv + q), y[ci[q]], acc);
+  for (int o = WIDE_LANES / 2; o > 0; o >>= 1) acc = acc + shfl_xor_any(acc, o);
+  if (t < m && lane == 0) y[s_tail + t] = y[s_tail + t] - acc;
+}
+// The sequential part of a tail sweep in one CTA; yt = y[s_tail..n) in
+// shared memory.  rows == nullptr: level l covers local rows lptr[l]..lptr[l+1].
+template <class S, class A>
+__global__ void __launch_bounds__(RUN_TPB) tail_run_kernel(int m, int s_tail, int nlev, const int* __restrict__ lptr,
+                                                          const int* __restrict__ rows, const int64_t* __restrict__ rp,
+                                                          const int* __restrict__ ci, const S* __restrict__ cv,
+                                                          A* __restrict__ y) {
+  extern __shared__ unsigned char smem_raw[];
+  A* yt = reinterpret_cast<A*>(smem_raw);
+  for (int t = threadIdx.x; t < m; t += RUN_TPB) yt[t] = y[s_tail + t];
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int l = 0; l < nlev; ++l) {
+    const int lo = lptr[l], hi = lptr[l + 1];
+    for (int t = lo + warp; t < hi; t += RUN_TPB / 32) {
+      const int r = rows ? rows[t] : t;
+      const int64_t b = rp[r], e = rp[r + 1];
+      A acc = A(0);
+      for (int64_t q = b + lane; q < e; q += 32) acc = fma_(ld_arith(cv + q), yt[ci[q]], acc);
+      acc = wsum(acc);
+      if (lane == 0) yt[r] = yt[r] - acc;
+    }
+    __syncthreads();
+  }
+  for (int t = threadIdx.x; t < m; t += RUN_TPB) y[s_tail + t] = yt[t];
+}
+
+// raise the dynamic shared-memory limit of the tail kernel once per size
+// (done before any graph capture: ildl_apply_graph calls it first)
+template <class S, class A> static void ensure_tail_smem(size_t bytes) {
+  static size_t set = 48 * 1024;
+  if (bytes > set) {
+    CK(cudaFuncSetAttribute(tail_run_kernel<S, A>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    set = bytes;
+  }
+}
+
+template <class S>
+void ildl_plan(DevFactor<S>& F, const std::vector<int64_t>& lp, const std::vector<int64_t>& up,
+               const std::vector<int>& brows) {
+  auto plan = [&](const std::vector<int>& ptr, bool fwd, std::vector<int>& seg) {
+    seg.clear();
+    const int nl = (int)ptr.size() - 1;
+    int l = 1;  // level 0 has no off-diagonal entries in either sweep
+    while (l < nl) {
+      auto work = [&](int lv) {
+        int64_t nz = 0;
+        for (int t = ptr[lv]; t < ptr[lv + 1]; ++t) {
+          int s = fwd ? t : brows[t];
+          nz += fwd ? (lp[s + 1] - lp[s]) : (up[s + 1] - up[s]);
+        }
+        return nz;
+      };
+      int rows = ptr[l + 1] - ptr[l];
+      int64_t nz = work(l);
+      bool narrow = rows <= 2048 && nz <= 65536;
+      if (!narrow) {
+        seg.insert(seg.end(), {l, l + 1, 0});
+        ++l;
+        continue;
+      }
+      int l1 = l + 1;
+      while (l1 < nl) {
+        int r = ptr[l1 + 1] - ptr[l1];
+        if (r > 2048 || work(l1) > 65536) break;
+        ++l1;
+      }
+      seg.insert(seg.end(), {l, l1, 1});
+      l = l1;
+    }
+  };
+  plan(F.fptr, true, F.fseg);
+  plan(F.bptr, false, F.bseg);
+}
+// levels of the bulk backward sweep start at 0 (rows may point into the tail)
+template <class S> void ildl_plan_bwd0(DevFactor<S>& F) {
+  std::vector<int> seg;
+  for (size_t q = 0; q < F.bseg.size(); q += 3) seg.insert(seg.end(), {F.bseg[q], F.bseg[q + 1], F.bseg[q + 2]});
+  if (F.bptr.size() > 1 && (F.bseg.empty() || F.bseg[0] != 0)) {
+    std::vector<int> s0 = {0, 1, 0};
+    s0.insert(s0.end(), seg.begin(), seg.end());
+    seg = s0;
+  }
+  F.bseg = seg;
+}
+
+template <class T, class S> void ildl_apply(const DevFactor<S>& F, bool spd, const T* b, T* x, cudaStream_t s) {
+  using A = typename Arith<S>::type;
+  const int n = F.n;
+  ildl_gather_kernel<T, A><<<nblk(n), TPB, 0, s>>>(n, F.orig, b, F.y);
+  auto sweep = [&](const std::vector<int>& seg, const std::vector<int>& ptr, const int* dptr, const int* rows,
+                   const int64_t* rp, const int* ci, const S* cv) {
+    for (size_t q = 0; q < seg.size(); q += 3) {
+      int l0 = seg[q], l1 = seg[q + 1];
+      if (seg[q + 2] == 1) {
+        ildl_run_kernel<S, A><<<1, RUN_TPB, 0, s>>>(l0, l1, dptr, rows, rp, ci, cv, F.y);
+      } else {
+        int lo = ptr[l0], hi = ptr[l0 + 1];
+        int nb = (hi - lo + WIDE_TPB / WIDE_LANES - 1) / (WIDE_TPB / WIDE_LANES);
+        ildl_wide_kernel<S, A><<<nb, WIDE_TPB, 0, s>>>(lo, hi, rows, rp, ci, cv, F.y);
+      }
+    }
+  };
+  sweep(F.fseg, F.fptr, F.dfptr, nullptr, F.lp, F.li, F.lx);
+  const size_t tsm = sizeof(A) * (size_t)std::max(F.m_tail, 1);
+  ensure_tail_smem<S, A>(tsm);
+  if (F.m_tail > 0) {
+    const int nb = (F.m_tail + WIDE_TPB / WIDE_LANES - 1) / (WIDE_TPB / WIDE_LANES);
+    tail_ext_kernel<S, A><<<nb, WIDE_TPB, 0, s>>>(F.m_tail, F.s_tail, F.tep, F.tei, F.tev, F.y);
+    tail_run_kernel<S, A><<<1, RUN_TPB, tsm, s>>>(F.m_tail, F.s_tail, (int)F.tfptr.size() - 1, F.dtfptr, nullptr,
+                                                 F.tip, F.tii, F.tiv, F.y);
+  }
+  ildl_dsolve_kernel<S, A><<<nblk(n), TPB, 0, s>>>(n, F.blk, F.partner, spd ? F.av : F.dv, spd ? F.aof : F.dof, F.y);
+  if (F.m_tail > 0)
+    tail_run_kernel<S, A><<<1, RUN_TPB, tsm, s>>>(F.m_tail, F.s_tail, (int)F.tbptr.size() - 1, F.dtbptr, F.tbrows,
+                                                 F.tbp, F.tbi, F.tbv, F.y);
+  sweep(F.bseg, F.bptr, F.dbptr, F.brows, F.up, F.ui, F.ux);
+  ildl_scatter_kernel<T, A><<<nblk(n), TPB, 0, s>>>(n, F.orig, F.y, x);
+}
+
+template <class T, class S> void ildl_apply_graph(DevFactor<S>& F, bool spd, const T* b, T* x, cudaStream_t s) {
+  const int n = F.n;
+  const int g = spd ? 1 : 0;
+  if (!F.graph[g]) {
+    ensure_tail_smem<S, typename Arith<S>::type>(sizeof(typename Arith<S>::type) * (size_t)std::max(F.m_tail, 1));
+    cudaGraph_t gr;
+    CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    ildl_apply<T, S>(F, spd, (const T*)F.rhs_in, (T*)F.sol_out, s);
+    CK(cudaStreamEndCapture(s, &gr));
+    size_t nn = 0;
+    CK(cudaGraphGetNodes(gr, nullptr, &nn));
+    F.graph_kernels[g] = (long long)nn;
+    CK(cudaGraphInstantiate(&F.graph[g], gr, 0));
+    CK(cudaGraphDestroy(gr));
+  }
+  if ((const void*)b != F.rhs_in) CK(cudaMemcpyAsync(F.rhs_in, b, sizeof(T) * n, cudaMemcpyDeviceToDevice, s));
+  CK(cudaGraphLaunch(F.graph[g], s));
+  g_launches += F.graph_kernels[g];
+  if ((void*)x != F.sol_out) CK(cudaMemcpyAsync(x, F.sol_out, sizeof(T) * n, cudaMemcpyDeviceToDevice, s));
+}
+
+// ------------------------------------------------------- instantiations ----
+#define JD_INST_T(T)                                                                               \
+  template void spmv<T>(const SellMatrix<T>&, const T*, T*, cudaStream_t);                         \
+  template void axpy<T>(long, T, const T*, T*, cudaStream_t);                                      \
+  template void scal<T>(long, double, T*, cudaStream_t);                                           \
+  template void fill<T>(long, T, T*, cudaStream_t);                                                \
+  template void mdot<T>(long, int, const T*, long, const T*, T*, T*, cudaStream_t);                \
+  template void gemv_dev<T>(long, int, T, const T*, long, const T*, T, T*, cudaStream_t);          \
+  template void gemv_val<T>(long, int, T, const T*, long, const T*, T, T*, cudaStream_t);          \
+  template void rmult<T>(long, int, int, const T*, long, const T*, T*, cudaStream_t);              \
+  template void diagsolve<T>(long, const double*, const T*, T*, cudaStream_t);
+JD_INST_T(double)
+JD_INST_T(zc)
+#define JD_INST_F(T, S)                                                                          \
+  template void ildl_apply<T, S>(const DevFactor<S>&, bool, const T*, T*, cudaStream_t);          \
+  template void ildl_apply_graph<T, S>(DevFactor<S>&, bool, const T*, T*, cudaStream_t);          \
+  template void ildl_plan<S>(DevFactor<S>&, const std::vector<int64_t>&, const std::vector<int64_t>&, \
+                             const std::vector<int>&);                                          \
+  template void ildl_plan_bwd0<S>(DevFactor<S>&);
+JD_INST_F(double, double)
+JD_INST_F(double, float)
+JD_INST_F(double, __nv_bfloat16)
+JD_INST_F(zc, zc)
+JD_INST_F(zc, cc)
+JD_INST_F(zc, bc)
+#if 0
+template void ildl_apply<double, double>(const DevFactor<double>&, bool, const double*, double*, cudaStream_t);
+template void ildl_apply<double, float>(const DevFactor<float>&, bool, const double*, double*, cudaStream_t);
+template void ildl_apply<double, __nv_bfloat16>(const DevFactor<__nv_bfloat16>&, bool, const double*, double*, cudaStream_t);
+template void ildl_apply<zc, zc>(const DevFactor<zc>&, bool, const zc*, zc*, cudaStream_t);
+template void ildl_apply<zc, cc>(const DevFactor<cc>&, bool, const zc*, zc*, cudaStream_t);
+template void ildl_apply<zc, bc>(const DevFactor<bc>&, bool, const zc*, zc*, cudaStream_t);
+#endif
+
+}  // namespace k
+}  // namespace jdg

@@ -1,0 +1,93 @@
+// Launch wrappers for the sm_103a kernels of the Jacobi-Davidson hot path.
+// Every wrapper enqueues on the given stream and never synchronises.
+#pragma once
+#include <vector>
+
+#include "common.cuh"
+
+namespace jdg {
+
+// Full Hermitian matrix in SELL-32 (slices of 32 rows, column-major inside a
+// slice, padded with the row's own index and a zero value).
+template <class T> struct SellMatrix {
+  int n = 0, nslices = 0;
+  int64_t nnz = 0;       // nonzeros of the full matrix (both triangles)
+  int64_t stored = 0;    // stored entries including padding
+  int64_t* sptr = nullptr;
+  int* col = nullptr;
+  T* val = nullptr;
+};
+
+// Level-scheduled factor on the device, in "solve numbering" s: rows of the
+// same forward level are contiguous; L^H rows are listed level by level in
+// brows.  S is the storage type, A = Arith<S>::type the arithmetic type.
+template <class S> struct DevFactor {
+  using A = typename Arith<S>::type;
+  int n = 0;
+  int64_t nnz_l = 0;
+  int* orig = nullptr;                       // orig[s]: row of the input vector
+  int64_t* lp = nullptr; int* li = nullptr; S* lx = nullptr;   // forward rows
+  int64_t* up = nullptr; int* ui = nullptr; S* ux = nullptr;   // rows of L^H (values conjugated)
+  int* brows = nullptr;
+  std::vector<int> fptr, bptr;               // level boundaries (host)
+  int* dfptr = nullptr; int* dbptr = nullptr; // the same on the device
+  // sweep segments: {first level, last level + 1, kind}; kind 0 = one grid
+  // launch per level, 1 = one single-CTA launch for the whole run of levels
+  std::vector<int> fseg, bseg;
+  signed char* blk = nullptr; int* partner = nullptr;
+  S *dv = nullptr, *dof = nullptr, *av = nullptr, *aof = nullptr;  // D^{-1} and |D|^{-1}
+  A* y = nullptr;                            // work vector
+  // captured launch sequence of one application (per spd flag), reading
+  // rhs_in and writing sol_out
+  // Tail: rows s >= s_tail (the deepest forward levels, m_tail rows) are
+  // solved by one CTA with the tail of y in shared memory.  Forward: the
+  // entries of tail rows that point below s_tail ("external") are applied by
+  // a grid kernel first; the rest ("internal", local column ids) level by
+  // level.  Backward: tail rows depend only on tail rows and are solved first;
+  // bptr/brows then list the remaining rows level by level.
+  int s_tail = 0, m_tail = 0;
+  int64_t* tep = nullptr; int* tei = nullptr; S* tev = nullptr;   // forward external
+  int64_t* tip = nullptr; int* tii = nullptr; S* tiv = nullptr;   // forward internal
+  int* dtfptr = nullptr; std::vector<int> tfptr;                  // forward tail levels (local rows)
+  int64_t* tbp = nullptr; int* tbi = nullptr; S* tbv = nullptr;   // backward tail rows of L^H (local)
+  int* dtbptr = nullptr; int* tbrows = nullptr; std::vector<int> tbptr;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  long long graph_kernels[2] = {0, 0};
+  void* rhs_in = nullptr;
+  void* sol_out = nullptr;
+};
+
+namespace k {
+
+// kernels launched by this library so far (graph replays count their kernel nodes)
+long long launch_count();
+void add_launches(long long n);
+
+template <class T> void spmv(const SellMatrix<T>& A, const T* x, T* y, cudaStream_t s);
+template <class T> void axpy(long n, T a, const T* x, T* y, cudaStream_t s);
+template <class T> void scal(long n, double a, T* x, cudaStream_t s);
+template <class T> void fill(long n, T v, T* x, cudaStream_t s);
+// out[c] = V(:,c)^H w for c < k (deterministic two-pass reduction); partial
+// needs mdot_partial_size(n,k) entries
+long mdot_partial_size(long n, int k);
+template <class T> void mdot(long n, int k, const T* V, long ldv, const T* w, T* out, T* partial, cudaStream_t s);
+// w = beta*w + alpha*V*y, y (k <= 64 entries) in device memory or by value
+template <class T> void gemv_dev(long n, int k, T alpha, const T* V, long ldv, const T* y, T beta, T* w, cudaStream_t s);
+template <class T> void gemv_val(long n, int k, T alpha, const T* V, long ldv, const T* y_host, T beta, T* w, cudaStream_t s);
+// out(:,c) = V * Q(:,c), c < keep, Q K x K column-major (host values)
+template <class T> void rmult(long n, int K, int keep, const T* V, long ldv, const T* Q_host, T* out, cudaStream_t s);
+// sol = d .* rhs (diagonal preconditioner, d real)
+template <class T> void diagsolve(long n, const double* d, const T* rhs, T* sol, cudaStream_t s);
+// preconditioner application  x = P (L D L^H)^{-1} P^T b  (|D| when spd)
+template <class T, class S> void ildl_apply(const DevFactor<S>& F, bool spd, const T* b, T* x, cudaStream_t s);
+// the same through the captured graph (builds it on first use); F.rhs_in and
+// F.sol_out must hold n entries of T
+template <class T, class S> void ildl_apply_graph(DevFactor<S>& F, bool spd, const T* b, T* x, cudaStream_t s);
+// split the level lists of F into wide levels and runs of narrow levels
+template <class S> void ildl_plan(DevFactor<S>& F, const std::vector<int64_t>& lp_host, const std::vector<int64_t>& up_host,
+                                  const std::vector<int>& brows_host);
+// make the bulk backward sweep start at level 0 (its rows may point into the tail)
+template <class S> void ildl_plan_bwd0(DevFactor<S>& F);
+
+}  // namespace k
+}  // namespace jdg

@@ -1,12 +1,14 @@
-// Test infrastructure only: small dense linear algebra for the CPU oracle.
+// Small dense linear algebra on the host for the J x J projected problems of
+// the Jacobi-Davidson loop (J <= MADSPACE, a few dozen at most).
 //
 // The reference calls LAPACK/BLAS for these (src/include/ilupackmacros.h:55-72,
-// used at src/jd/JDaux.F:1651-1659, 2027-2031, 2430-2449, 3294-3331); no LAPACK
-// is available here, so the oracle restates each operation from its definition:
-// Hermitian eigenproblems by cyclic Jacobi, Cholesky, Householder QR, and the
-// BLAS-2/3 products the JD loop uses.  Column-major storage with a leading
-// dimension, as in the reference workspace.  Only tests, the smoke check and
-// the CPU-baseline leg of bench.py load this code.
+// used at src/jd/JDaux.F:1651-1659, 2027-2031, 2430-2449, 3294-3331).  No
+// LAPACK is linked; each operation is written from its definition: Hermitian
+// eigenproblems by cyclic Jacobi, Cholesky, Householder QR, and the BLAS-2/3
+// products on J x J data.  Column-major storage with a leading dimension, as
+// in the reference workspace.  The N-length vector helpers (dotc, nrm2, axpy,
+// gemv_*) are used by the CPU oracle only; the GPU library runs those on the
+// device.
 #pragma once
 #include <algorithm>
 #include <cmath>
@@ -15,7 +17,7 @@
 #include <numeric>
 #include <vector>
 
-namespace orc {
+namespace jdd {
 
 using cplx = std::complex<double>;
 inline double re(double x) { return x; }
@@ -268,4 +270,4 @@ inline void sort_index(long n, const double* key, long* idx) {
   std::stable_sort(idx, idx + n, [&](long a, long b) { return key[a] < key[b]; });
 }
 
-}  // namespace orc
+}  // namespace jdd

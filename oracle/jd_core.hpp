@@ -19,9 +19,10 @@
 #include <cstdio>
 #include <vector>
 
-#include "dense.hpp"
+#include "../jadamilu_gb300/csrc/small_dense.hpp"
 
 namespace orc {
+using namespace jdd;
 
 // Values that JDRVCOM shares with the preconditioner-aware driver through
 // the COMMON block /JDRVCOMJD/ (JDaux.F:47-48).

@@ -28,6 +28,9 @@
 
 namespace orc {
 
+// ordering weight of the triangular-solve depth (same default as the GPU library)
+static double g_depth_weight = 64.0;
+
 static double now_s() {
   using namespace std::chrono;
   return duration<double>(steady_clock::now().time_since_epoch()).count();
@@ -258,6 +261,7 @@ int pjdinit(Global<T>& g, int n, T* a, int* ja, int* ia, const T* b, const int* 
     const int recompilu = (icntl[1] == 0 || icntl[1] == -2) ? 1 : -1;
     const double nposeig = (icntl[2] <= 0) ? 0.01 : 0.0;
     jdg::IldlcParams prm;
+    prm.depth_weight = g_depth_weight;
     prm.droptol = DROPTOL;
     prm.condest = condest;
     prm.mem = MEM;
@@ -593,6 +597,33 @@ void orc_zpjd(int n, cplx* a, int* ja, int* ia, cplx* b, int* jb, int* ib, doubl
                  *shift, *droptol, *mem, icntl, *info, *gap, gep != 0, user_mv, user_ctx);
 }
 void orc_dpjdcleanup(void) { orc::G<double>().cleanup1(); }
+
+// Install an externally computed factor (same data layout as the project's
+// host factor) as the current preconditioner, for runs with ICNTL(2) = -1.
+void orc_dimport_factor(int n, const int* perm, const long long* lp, const int* li, const double* lx,
+                        const signed char* blk, const double* dinv, const double* doff, const double* ainv,
+                        const double* aoff, double shift0) {
+  auto& g = orc::G<double>();
+  g.cleanup1();
+  auto& F = g.F;
+  F.n = n;
+  F.perm.assign(perm, perm + n);
+  F.lp.assign(lp, lp + n + 1);
+  F.li.assign(li, li + lp[n]);
+  F.lx.assign(lx, lx + lp[n]);
+  F.blk.assign(blk, blk + n);
+  F.dinv.assign(dinv, dinv + n);
+  F.doff.assign(doff, doff + n);
+  F.ainv.assign(ainv, ainv + n);
+  F.aoff.assign(aoff, aoff + n);
+  F.level_start = {0, n};
+  F.nnz_a_upper = 1;
+  g.factdgl = -1;
+  g.shift0 = shift0;
+  g.timefact = 1.0;
+  g.factspd = 0;
+  g.memused = g.memrequested = 1e30;
+}
 void orc_zpjdcleanup(void) { orc::G<cplx>().cleanup1(); }
 int orc_nfactor_d(void) { return orc::G<double>().nfactor; }
 
@@ -607,10 +638,15 @@ void orc_zmatveca(int n, const int* ia, const int* ja, const cplx* a, const cplx
 // Factor (the project's host code) + the oracle's application of it, on an
 // opaque handle, for kernel-level parity of the GPU preconditioner.
 struct OrcFactorD { jdg::IldlcFactor<double> F; };
+void orc_set_depth_weight(double w) { orc::g_depth_weight = w; }
+static double g_dropS = -1;
+void orc_set_drop_schur(double v) { g_dropS = v; }
 void* orc_dfactor(int n, const int* ia, const int* ja, const double* a, double shift, double droptol, double condest,
                   double mem, int* ierr) {
   auto* h = new OrcFactorD;
   jdg::IldlcParams p;
+  p.depth_weight = orc::g_depth_weight;
+  p.droptol_schur = g_dropS;
   p.droptol = droptol;
   p.condest = condest;
   p.mem = mem;
@@ -630,6 +666,16 @@ void orc_dfactor_info(void* h, long* out) {
   long n2 = 0;
   for (int p = 0; p < F.n; ++p) n2 += F.blk[p] == 2;
   out[6] = n2;
+}
+// per elimination step: forward level; level_start boundaries into ls (size nlevels+1)
+void orc_dfactor_levels(void* h, int* flev, int* ls) {
+  auto& F = ((OrcFactorD*)h)->F;
+  for (int p = 0; p < F.n; ++p) {
+    int m = 0;
+    for (int64_t q = F.lp[p]; q < F.lp[p + 1]; ++q) m = std::max(m, flev[F.li[q]] + 1);
+    flev[p] = m;
+  }
+  for (size_t i = 0; i < F.level_start.size(); ++i) ls[i] = F.level_start[i];
 }
 void orc_dfactor_apply(void* h, int spd, int single, const double* b, double* x) {
   auto& F = ((OrcFactorD*)h)->F;

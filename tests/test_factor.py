@@ -1,0 +1,72 @@
+"""The host multilevel ILDLC factorisation (project code, no GPU)."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from jadamilu_gb300 import matrices as M
+
+
+def _random_indefinite(n, seed):
+    rng = np.random.default_rng(seed)
+    A = sp.random(n, n, density=6.0 / n, random_state=seed)
+    A = A + A.T + sp.diags(rng.uniform(-2, 2, n))
+    U = sp.triu(A).tocsr()
+    U.sort_indices()
+    # diagonal must be present in every row
+    U = (U + sp.diags(np.where(U.diagonal() == 0, 1e-3, 0.0))).tocsr()
+    rows = np.repeat(np.arange(n), np.diff(U.indptr))
+    return (U.indptr + 1).astype(np.int32), (U.indices + 1).astype(np.int32), U.data.astype(np.float64)
+
+
+CASES = {
+    "laplace6": lambda: M.laplace3d(6),
+    "anderson7": lambda: M.anderson3d(7, seed=2),
+    "tridiag": lambda: M.tridiag(300),
+    "tridiag_zero_diag": lambda: M.tridiag(300, diag_scale=0.0),
+    "random_indefinite": lambda: _random_indefinite(400, 7),
+}
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_exact_when_nothing_is_dropped(oracle, name):
+    ia, ja, a = CASES[name]()
+    A = M.to_scipy_full(ia, ja, a)
+    F = oracle.Factor(ia, ja, a, shift=0.1, droptol=0.0, mem=0)
+    assert F.ierr == 0
+    b = np.random.default_rng(1).standard_normal(A.shape[0])
+    x = F.apply(b)
+    As = A - 0.1 * sp.eye(A.shape[0])
+    assert np.linalg.norm(As @ x - b) <= 1e-9 * np.linalg.norm(b) * max(1, np.abs(As).max())
+
+
+def test_two_by_two_pivots_and_levels(oracle):
+    ia, ja, a = M.anderson3d(8, seed=3)
+    F = oracle.Factor(ia, ja, a, shift=0.0, droptol=1e-3)
+    info = F.info()
+    assert info["n2x2"] > 0          # indefinite: some 2x2 pivots
+    assert info["nlevels"] >= 2      # deferred rows formed Schur levels
+    assert info["nneg"] > 0
+
+
+def test_spd_conversion_gives_spd_preconditioner(oracle):
+    ia, ja, a = M.anderson3d(6, seed=4)
+    F = oracle.Factor(ia, ja, a, shift=0.0, droptol=1e-3)
+    n = F.n
+    Mi = np.stack([F.apply(e, spd=True) for e in np.eye(n)], 1)
+    np.testing.assert_allclose(Mi, Mi.T, atol=1e-10 * np.abs(Mi).max())
+    assert np.linalg.eigvalsh(0.5 * (Mi + Mi.T)).min() > 0
+
+
+def test_single_precision_apply_close(oracle):
+    ia, ja, a = M.anderson3d(8, seed=3)
+    F = oracle.Factor(ia, ja, a, shift=0.0, droptol=1e-3)
+    b = np.random.default_rng(0).standard_normal(F.n)
+    x64 = F.apply(b)
+    x32 = F.apply(b, single=True)
+    assert np.linalg.norm(x32 - x64) <= 1e-4 * np.linalg.norm(x64)
+
+
+def test_memory_limit_reports_error(oracle):
+    ia, ja, a = M.anderson3d(8, seed=3)
+    F = oracle.Factor(ia, ja, a, shift=0.0, droptol=0.0, mem=1.5)
+    assert F.ierr == -3

@@ -1,0 +1,136 @@
+"""End-to-end parity of the GPU drivers (through the C ABI) with the oracle.
+
+Eigenvalues must agree with the oracle and the reference's printed values
+within 1e-10 relative (absolute 1e-12 for the O(1) user-guide samples), and
+residual norms must meet TOL.
+"""
+import numpy as np
+import pytest
+
+from jadamilu_gb300 import matrices as M
+from problems import dense_eigs, kat_problem
+
+pytestmark = pytest.mark.gpu
+
+
+def _close(a, b, rel=1e-10, floor=1e-12):
+    a, b = np.sort(a), np.sort(b)
+    assert a.shape == b.shape
+    assert np.all(np.abs(a - b) <= np.maximum(rel * np.abs(b), floor)), (a, b)
+
+
+@pytest.mark.parametrize("name", ["EXAMPLE1", "EXAMPLE2", "EXAMPLE5", "EXAMPLE6", "EXAMPLE9", "EXAMPLE10"])
+def test_userguide_samples(gpu, oracle, kats, name):
+    meta = kats[name]
+    A, As, mv, kw = kat_problem(meta)
+    if meta["driver"] == "dpjd":
+        r = gpu.dpjd((A[2], A[1], A[0]), 5, **kw)
+        ro = oracle.dpjd(*A, 5, **kw)
+    elif meta["driver"] == "dpjdrevcom":
+        r = gpu.dpjdrevcom((A[2], A[1], A[0]), 5, mv, **kw)
+        ro = oracle.dpjd(*A, 5, user_matvec=mv, **kw)
+    else:
+        d = As.diagonal().copy()
+        neg = np.full(len(d) + 1, -1, np.int32)
+        r = gpu.dpjdrevcom((d, neg, neg), 5, mv, **kw)
+        ro = oracle.dpjd(neg, neg, d, 5, user_matvec=mv, **kw)
+    assert r["info"] == 0 and r["neig"] == 5
+    np.testing.assert_allclose(r["eigs"], meta["eigenvalues"], rtol=0, atol=1e-12)
+    _close(r["eigs"], ro["eigs"])
+    assert np.all(r["res"] <= 1e-10)
+    # eigenvectors: unit norm, residual checked independently
+    for k in range(5):
+        x = r["x"][:, k]
+        assert abs(np.linalg.norm(x) - 1) < 1e-10
+        assert np.linalg.norm(mv(x) - r["eigs"][k] * x) < 1e-9
+
+
+def test_laplace_20_cubed_plain_fp64(gpu, oracle):
+    """Laplacian 20^3 (n=8000), 10 smallest, TOL 1e-10, DROPTOL 1e-3, FP64."""
+    ia, ja, a = M.laplace3d(20)
+    kw = dict(isearch=0, madspace=20, maxit=2000, tol=1e-10, droptol=1e-3, mem=20.0)
+    r = gpu.dpjd((a, ja, ia), 10, **kw)
+    assert r["info"] == 0 and r["neig"] == 10
+    exact = M.laplace3d_eigenvalues(20, 10)
+    _close(r["eigs"], exact)
+    assert np.all(r["res"] <= 1e-10)
+    ro = oracle.dpjd(ia, ja, a, 10, **kw)
+    _close(r["eigs"], ro["eigs"])
+
+
+@pytest.mark.parametrize("precision", [0, 1, 2])
+def test_anderson_interior(gpu, oracle, precision):
+    ia, ja, a = M.anderson3d(12, seed=7)
+    As = M.to_scipy_full(ia, ja, a)
+    kw = dict(isearch=2, sigma=0.0, madspace=25, maxit=4000, tol=1e-10, droptol=1e-3, mem=40.0,
+              icntl=(0, 1, 0, 0, precision))
+    r = gpu.dpjd((a, ja, ia), 8, **kw)
+    assert r["info"] == 0 and r["neig"] == 8
+    _close(r["eigs"], dense_eigs(As, 8, 0.0))
+    assert np.all(r["res"] <= 1e-10)
+    if precision < 2:
+        ro = oracle.dpjd(ia, ja, a, 8, **kw)
+        _close(r["eigs"], ro["eigs"])
+
+
+def test_complex_hermitian(gpu, oracle):
+    ia, ja, a = M.tight_binding3d(8, seed=1)
+    As = M.to_scipy_full(ia, ja, a)
+    kw = dict(isearch=0, madspace=20, maxit=2000, tol=1e-10, droptol=1e-3, icntl=(0, 1, 0, 0, 1))
+    r = gpu.zpjd((a, ja, ia), 6, **kw)
+    assert r["info"] == 0 and r["neig"] == 6
+    _close(r["eigs"], dense_eigs(As, 6))
+    ro = oracle.dpjd(ia, ja, a, 6, complex_=True, **kw)
+    _close(r["eigs"], ro["eigs"])
+
+
+def test_generalized(gpu, oracle):
+    import scipy.linalg as sl
+    K, Mm = M.fem_p1(16, seed=3)
+    kw = dict(isearch=0, madspace=16, maxit=2000, tol=1e-9, droptol=1e-3)
+    r = gpu.dpjd_gep((K[2], K[1], K[0]), (Mm[2], Mm[1], Mm[0]), 4, **kw)
+    assert r["info"] == 0 and r["neig"] == 4
+    w = sl.eigh(M.to_scipy_full(*K).toarray(), M.to_scipy_full(*Mm).toarray(), eigvals_only=True)[:4]
+    _close(r["eigs"], w, rel=1e-9)
+    ro = oracle.dpjd(*K, 4, b=Mm, **kw)
+    _close(r["eigs"], ro["eigs"], rel=1e-9)
+
+
+def test_djdrevcom_user_preconditioner(gpu):
+    """DJDREVCOM with a user matvec and user preconditioner (EXAMPLE8 style)."""
+    n = 1000
+    import scipy.sparse as sp
+    main = 4 * np.ones(n)
+    A = sp.diags([main, -np.ones(n - 1), -np.ones(n - 1)], [0, -1, 1]).tolil()
+    A[0, n - 1] = A[n - 1, 0] = -1
+    A = A.tocsr()
+    # the banded approximate inverse of samples/EXAMPLE8.f:73-87 (circulant)
+    def prec(y):
+        return (16 * y + 4 * (np.roll(y, 1) + np.roll(y, -1)) + (np.roll(y, 2) + np.roll(y, -2))) / 64.0
+    r = gpu.djdrevcom(n, 5, lambda x: A @ x, prec, isearch=0, madspace=20, maxit=4000, tol=1e-10)
+    assert r["info"] == 0 and r["neig"] == 5
+    w = np.linalg.eigvalsh(A.toarray())[:5]
+    _close(r["eigs"], w)
+
+
+@pytest.mark.parametrize("case,info", [("neig", -5), ("madspace", -9), ("iter", -11), ("tol", -12)])
+def test_info_codes(gpu, case, info):
+    kw = dict(isearch=0, madspace=10, maxit=100, tol=1e-8)
+    neig = 3
+    if case == "neig":
+        neig = 0
+    elif case == "madspace":
+        kw["madspace"] = 2
+    elif case == "iter":
+        kw["maxit"] = 0
+    elif case == "tol":
+        kw["tol"] = 0.0
+    ia, ja, a = M.tridiag(60)
+    r = gpu.dpjd((a, ja, ia), neig, **kw)
+    assert r["info"] == info
+
+
+def test_maxit_returns_partial(gpu):
+    ia, ja, a = M.laplace3d(8)
+    r = gpu.dpjd((a, ja, ia), 10, isearch=0, madspace=10, maxit=25, tol=1e-12, droptol=1e-1)
+    assert r["info"] > 0

@@ -1,0 +1,63 @@
+"""Kernel parity: GPU SpMV and GPU preconditioner application vs the oracle."""
+import numpy as np
+import pytest
+
+from jadamilu_gb300 import matrices as M
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("gen", [lambda: M.laplace3d(12), lambda: M.anderson3d(15, seed=1),
+                                 lambda: M.tridiag(1000), lambda: M.fem_p1(40)[0]])
+def test_spmv_real(gpu, oracle, gen):
+    ia, ja, a = gen()
+    n = len(ia) - 1
+    x = np.random.default_rng(0).standard_normal(n)
+    y = gpu.spmv((a, ja, ia), x)
+    yo = np.zeros(n)
+    import ctypes as C
+    p = lambda v: v.ctypes.data_as(C.c_void_p)
+    oracle.lib().orc_dmatveca(n, p(ia), p(ja), p(a), p(x), p(yo))
+    np.testing.assert_allclose(y, yo, rtol=1e-13, atol=1e-13 * np.abs(yo).max())
+
+
+def test_spmv_complex(gpu, oracle):
+    import ctypes as C
+    ia, ja, a = M.tight_binding3d(10, seed=1)
+    n = len(ia) - 1
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    y = gpu.spmv((a, ja, ia), x)
+    yo = np.zeros(n, np.complex128)
+    p = lambda v: v.ctypes.data_as(C.c_void_p)
+    oracle.lib().orc_zmatveca(n, p(ia), p(ja), p(a), p(x), p(yo))
+    np.testing.assert_allclose(y, yo, rtol=1e-13, atol=1e-13 * np.abs(yo).max())
+
+
+@pytest.mark.parametrize("spd", [False, True])
+@pytest.mark.parametrize("precision,tol", [(0, 1e-11), (1, 2e-5)])
+@pytest.mark.parametrize("gen,shift", [(lambda: M.anderson3d(12, seed=2), 0.0), (lambda: M.laplace3d(12), 10.0),
+                                       (lambda: M.tridiag(2000), 0.0)])
+def test_ildl_apply_matches_oracle(gpu, oracle, gen, shift, spd, precision, tol):
+    ia, ja, a = gen()
+    n = len(ia) - 1
+    F = oracle.Factor(ia, ja, a, shift=shift, droptol=1e-3, mem=0)
+    assert F.ierr == 0
+    B = np.random.default_rng(3).standard_normal((2, n))
+    Xg, info = gpu.ildl_apply((a, ja, ia), B, shift=shift, droptol=1e-3, spd=spd, precision=precision)
+    fi = F.info()
+    assert info["nnz_l"] == fi["nnz_l"] and info["fwd_depth"] == fi["fwd_depth"]
+    for r in range(2):
+        xo = F.apply(B[r], spd=spd, single=(precision == 1))
+        err = np.linalg.norm(Xg[r] - xo) / np.linalg.norm(xo)
+        assert err <= tol, err
+
+
+def test_ildl_apply_bf16_is_a_preconditioner(gpu, oracle):
+    ia, ja, a = M.laplace3d(12)
+    n = len(ia) - 1
+    F = oracle.Factor(ia, ja, a, shift=0.0, droptol=1e-3, mem=0)
+    b = np.random.default_rng(3).standard_normal(n)
+    xb, _ = gpu.ildl_apply((a, ja, ia), b, shift=0.0, spd=True, precision=2)
+    xo = F.apply(b, spd=True)
+    assert np.linalg.norm(xb - xo) / np.linalg.norm(xo) < 5e-2
