@@ -18,13 +18,13 @@ namespace jdg {
 
 struct alignas(16) zc {
   double x, y;
-  JD_HD zc() : x(0), y(0) {}
+  zc() = default;
   JD_HD zc(double r) : x(r), y(0) {}
   JD_HD zc(double r, double i) : x(r), y(i) {}
 };
 struct alignas(8) cc {
   float x, y;
-  JD_HD cc() : x(0), y(0) {}
+  cc() = default;
   JD_HD cc(float r) : x(r), y(0) {}
   JD_HD cc(float r, float i) : x(r), y(i) {}
 };

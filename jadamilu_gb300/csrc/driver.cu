@@ -147,7 +147,8 @@ template <class S, class H> void upload_factor(const IldlcFactor<H>& F, DevFacto
   // tail: the deepest run of narrow levels, as long as its part of y fits in
   // shared memory
   using A = typename DevFactor<S>::A;
-  const int tail_max = std::min<int>(16384, (int)((200 * 1024) / sizeof(A)));
+  // per tail row: its y entry, a row pointer, a level pointer and a row index
+  const int tail_max = std::min<int>(16384, (int)((200 * 1024) / (sizeof(A) + 12)));
   int Lt = nfl, acc_rows = 0;
   while (Lt > 1) {
     int r = fptr[Lt] - fptr[Lt - 1];

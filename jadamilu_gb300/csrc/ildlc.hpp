@@ -28,7 +28,10 @@
 #include <cmath>
 #include <complex>
 #include <cstdint>
+#include <atomic>
 #include <cstring>
+#include <functional>
+#include <thread>
 #include <vector>
 
 namespace jdg {
@@ -50,6 +53,7 @@ struct IldlcParams {
   int last_level_min = 64; // a deferred set this small becomes the last level
   double min_progress = 0.05;  // a level accepting fewer than this fraction ends the recursion
   double depth_weight = 64.0;  // ordering key = degree + depth_weight * (forward level of the row)
+  int threads = 0;             // host threads for the row updates (0: hardware concurrency, at most 16)
 };
 
 template <class T> struct IldlcFactor {
@@ -133,6 +137,64 @@ struct DegQueue {
     remove(i);
     return i;
   }
+};
+
+// Fork-join pool for the row updates of one pivot: run(count, f) calls
+// f(tid, i) for i in [0, count) spread over the threads, the caller
+// included, and returns when all are done.  Workers spin between jobs.
+class RowPool {
+ public:
+  explicit RowPool(int nthreads) : nt_(std::max(1, nthreads)) {
+    for (int t = 1; t < nt_; ++t) th_.emplace_back([this, t] { loop(t); });
+  }
+  ~RowPool() {
+    stop_.store(true);
+    gen_.fetch_add(1);
+    for (auto& t : th_) t.join();
+  }
+  int size() const { return nt_; }
+  template <class F> void run(int count, F&& f) {
+    if (nt_ == 1 || count < 2 * nt_) {
+      for (int i = 0; i < count; ++i) f(0, i);
+      return;
+    }
+    job_ = [&f](int tid, int i) { f(tid, i); };
+    count_ = count;
+    next_.store(0);
+    done_.store(0);
+    gen_.fetch_add(1, std::memory_order_release);
+    work(0);
+    while (done_.load(std::memory_order_acquire) < nt_ - 1) {
+    }
+  }
+
+ private:
+  void work(int tid) {
+    for (;;) {
+      int i = next_.fetch_add(1);
+      if (i >= count_) break;
+      job_(tid, i);
+    }
+  }
+  void loop(int tid) {
+    long seen = 0;
+    for (;;) {
+      long g;
+      while ((g = gen_.load(std::memory_order_acquire)) == seen) {
+      }
+      seen = g;
+      if (stop_.load()) return;
+      work(tid);
+      done_.fetch_add(1, std::memory_order_release);
+    }
+  }
+  int nt_;
+  std::vector<std::thread> th_;
+  std::atomic<long> gen_{0};
+  std::atomic<int> next_{0}, done_{0};
+  std::atomic<bool> stop_{false};
+  int count_ = 0;
+  std::function<void(int, int)> job_;
 };
 
 }  // namespace detail
@@ -227,6 +289,13 @@ int ildlc_factor(int n, const int* ia, const int* ja, const T* a, double shift, 
   std::vector<double> sc(n, 1.0), xi(n, 0.0);
   std::vector<cplx> xic(n, cplx(0));  // complex estimator accumulators
   std::vector<int> slot(n, -1);
+  const int nthr = prm.threads > 0 ? prm.threads
+                                   : (int)std::min<unsigned>(16, std::max(1u, std::thread::hardware_concurrency()));
+  RowPool pool(n >= 20000 ? nthr : 1);
+  std::vector<std::vector<int>> tslot(pool.size());
+  for (auto& v : tslot) v.assign(n, -1);
+  std::vector<char> inkept(n, 0);
+  std::vector<int> nbr;
   std::vector<int> dlev(n, 0);  // forward level row i would get if eliminated now
   auto qkey = [&](int i) { return (int)A.rows[i].size() + (int)(prm.depth_weight * dlev[i]); };
   std::vector<int> level_nodes(n);
@@ -356,24 +425,38 @@ int ildlc_factor(int n, const int* ia, const int* ja, const T* a, double shift, 
             }
           }
         }
-        // Schur update a_ij -= l_ik d conj(l_jk)
-        for (size_t q = 0; q < kept.size(); ++q) {
+        // Schur update a_ij -= l_ik d conj(l_jk); each row has one owner
+        // thread.  Neighbours whose L entry was dropped only lose column k.
+        for (size_t q = 0; q < kept.size(); ++q) inkept[kept[q]] = 1;
+        nbr.clear();
+        for (auto& e : A.rows[k])
+          if (!inkept[e.col] && state[e.col] != 1) nbr.push_back(e.col);
+        const int nkept = (int)kept.size();
+        pool.run(nkept + (int)nbr.size(), [&](int tid, int q) {
+          if (q >= nkept) {
+            remove_col(nbr[q - nkept], k);
+            return;
+          }
+          int* sl = tslot[tid].data();
           int i = kept[q];
           auto& row = A.rows[i];
-          for (size_t t = 0; t < row.size(); ++t) slot[row[t].col] = (int)t;
+          for (size_t t = 0; t < row.size(); ++t) sl[row[t].col] = (int)t;
           T li = lk[q];
           A.diag[i] -= T(fre(li * d * fcj(li)));
           for (size_t t = 0; t < kept.size(); ++t) {
-            if (t == q) continue;
+            if (t == (size_t)q) continue;
             int j = kept[t];
             T u = li * d * fcj(lk[t]);
-            if (slot[j] >= 0) row[slot[j]].val -= u;
-            else if (fab(u) * sc[i] * sc[j] > dropS) { row.push_back({j, -u}); slot[j] = (int)row.size() - 1; }
+            if (sl[j] >= 0) row[sl[j]].val -= u;
+            else if (fab(u) * sc[i] * sc[j] > dropS) { row.push_back({j, -u}); sl[j] = (int)row.size() - 1; }
           }
-          for (auto& e : row) slot[e.col] = -1;
+          for (auto& e : row) sl[e.col] = -1;
+          remove_col(i, k);
+        });
+        for (int i : kept) {
+          dlev[i] = std::max(dlev[i], dlev[k] + 1);
+          inkept[i] = 0;
         }
-        for (int i : kept) dlev[i] = std::max(dlev[i], dlev[k] + 1);
-        for (auto& e : A.rows[k]) remove_col(e.col, k);
         pos[k] = (int)order.size();
         order.push_back(k);
         blk[pos[k]] = 1;
@@ -455,21 +538,23 @@ int ildlc_factor(int n, const int* ia, const int* ja, const T* a, double shift, 
         std::vector<int> act;
         for (size_t q = 0; q < nb.size(); ++q)
           if (keepk[q] || keepj[q]) act.push_back((int)q);
-        for (int qa : act) {
+        pool.run((int)act.size(), [&](int tid, int qq) {
+          int* sl = tslot[tid].data();
+          const int qa = act[qq];
           int i = nb[qa];
           auto& row = A.rows[i];
-          for (size_t t = 0; t < row.size(); ++t) slot[row[t].col] = (int)t;
+          for (size_t t = 0; t < row.size(); ++t) sl[row[t].col] = (int)t;
           for (int ta : act) {
             int l = nb[ta];
             T c0 = fcj(lk[ta]), c1 = fcj(lj[ta]);
             T t0 = dkk * c0 + akj * c1, t1 = fcj(akj) * c0 + djj * c1;
             T u = lk[qa] * t0 + lj[qa] * t1;
             if (l == i) { A.diag[i] -= T(fre(u)); continue; }
-            if (slot[l] >= 0) row[slot[l]].val -= u;
-            else if (fab(u) * sc[i] * sc[l] > dropS) { row.push_back({l, -u}); slot[l] = (int)row.size() - 1; }
+            if (sl[l] >= 0) row[sl[l]].val -= u;
+            else if (fab(u) * sc[i] * sc[l] > dropS) { row.push_back({l, -u}); sl[l] = (int)row.size() - 1; }
           }
-          for (auto& e : row) slot[e.col] = -1;
-        }
+          for (auto& e : row) sl[e.col] = -1;
+        });
         {
           int lv = std::max(dlev[k], dlev[j]) + 1;
           for (size_t q = 0; q < nb.size(); ++q)

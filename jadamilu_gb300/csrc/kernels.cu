@@ -259,23 +259,48 @@ __device__ __forceinline__ cc wsum(cc v) { return cc(wsum(v.x), wsum(v.y)); }
 __device__ __forceinline__ zc wsum(zc v) { return zc(wsum(v.x), wsum(v.y)); }
 
 constexpr int RUN_TPB = 1024;
+constexpr int RUN_WARPS = RUN_TPB / 32;
+// A level with R < 32 rows gives each row 32/R warps; their partial sums are
+// added in a fixed order after a barrier, so results do not depend on timing.
 template <class S, class A>
 __global__ void __launch_bounds__(RUN_TPB) ildl_run_kernel(int l0, int l1, const int* __restrict__ lptr,
                                                           const int* __restrict__ rows, const int64_t* __restrict__ rp,
                                                           const int* __restrict__ ci, const S* __restrict__ cv,
                                                           A* y) {
+  __shared__ A part[RUN_WARPS];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int l = l0; l < l1; ++l) {
-    const int lo = lptr[l], hi = lptr[l + 1];
-    for (int t = lo + warp; t < hi; t += RUN_TPB / 32) {
-      const int s = rows ? rows[t] : t;
-      const int64_t b = rp[s], e = rp[s + 1];
+    const int lo = lptr[l], hi = lptr[l + 1], R = hi - lo;
+    if (R >= RUN_WARPS) {
+      for (int t = lo + warp; t < hi; t += RUN_WARPS) {
+        const int s = rows ? rows[t] : t;
+        const int64_t b = rp[s], e = rp[s + 1];
+        A acc = A(0);
+        for (int64_t q = b + lane; q < e; q += 32) acc = fma_(ld_arith(cv + q), y[ci[q]], acc);
+        acc = wsum(acc);
+        if (lane == 0) y[s] = y[s] - acc;
+      }
+      __syncthreads();
+    } else {
+      int G = RUN_WARPS / R;
+      G = 1 << (31 - __clz(G));
+      const int slot = warp / G, sub = warp % G;
       A acc = A(0);
-      for (int64_t q = b + lane; q < e; q += 32) acc = fma_(ld_arith(cv + q), y[ci[q]], acc);
+      int s = -1;
+      if (slot < R) {
+        s = rows ? rows[lo + slot] : lo + slot;
+        for (int64_t q = rp[s] + sub * 32 + lane; q < rp[s + 1]; q += 32 * G) acc = fma_(ld_arith(cv + q), y[ci[q]], acc);
+      }
       acc = wsum(acc);
-      if (lane == 0) y[s] = y[s] - acc;
+      if (lane == 0) part[warp] = acc;
+      __syncthreads();
+      if (slot < R && sub == 0 && lane == 0) {
+        A t = part[warp];
+        for (int j = 1; j < G; ++j) t = t + part[warp + j];
+        y[s] = y[s] - t;
+      }
+      __syncthreads();
     }
-    __syncthreads();
   }
 }
 // One wide level: 8 lanes per row.
@@ -312,29 +337,107 @@ __global__ void __launch_bounds__(WIDE_TPB) tail_ext_kernel(int m, int s_tail, c
   for (int o = WIDE_LANES / 2; o > 0; o >>= 1) acc = acc + shfl_xor_any(acc, o);
   if (t < m && lane == 0) y[s_tail + t] = y[s_tail + t] - acc;
 }
-// The sequential part of a tail sweep in one CTA; yt = y[s_tail..n) in
-// shared memory.  rows == nullptr: level l covers local rows lptr[l]..lptr[l+1].
+// The sequential part of a tail sweep in one CTA.  Shared memory holds the
+// tail of y (yt), the row pointers relative to the first tail entry, the level
+// pointers and (backward sweep) the row order, so a level costs one global
+// load of entries, which is issued for the next level before the barrier.
+// Rows of small levels are split over several warps as in ildl_run_kernel.
+template <class A> __host__ __device__ constexpr size_t tail_smem_bytes(int m, int nlev, bool rows) {
+  return ((sizeof(A) * (size_t)m + 15) / 16) * 16 + 4 * (size_t)(m + 1) + 4 * (size_t)(nlev + 1) +
+         (rows ? 4 * (size_t)m : 0);
+}
 template <class S, class A>
 __global__ void __launch_bounds__(RUN_TPB) tail_run_kernel(int m, int s_tail, int nlev, const int* __restrict__ lptr,
                                                           const int* __restrict__ rows, const int64_t* __restrict__ rp,
                                                           const int* __restrict__ ci, const S* __restrict__ cv,
                                                           A* __restrict__ y) {
-  extern __shared__ unsigned char smem_raw[];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
   A* yt = reinterpret_cast<A*>(smem_raw);
-  for (int t = threadIdx.x; t < m; t += RUN_TPB) yt[t] = y[s_tail + t];
+  int* srp = reinterpret_cast<int*>(smem_raw + ((sizeof(A) * (size_t)m + 15) / 16) * 16);
+  int* slp = srp + (m + 1);
+  int* srw = slp + (nlev + 1);
+  __shared__ A part[RUN_WARPS];
+  const int64_t base = rp[0];
+  for (int t = threadIdx.x; t < m; t += RUN_TPB) {
+    yt[t] = y[s_tail + t];
+    if (rows) srw[t] = rows[t];
+  }
+  for (int t = threadIdx.x; t <= m; t += RUN_TPB) srp[t] = (int)(rp[t] - base);
+  for (int t = threadIdx.x; t <= nlev; t += RUN_TPB) slp[t] = lptr[t];
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // this warp's row r, entry range [q0, q1) with stride `step` in level l
+  auto assign = [&](int l, int& r, int& q0, int& q1, int& step, int& G, int& slot, int& sub) {
+    const int lo = slp[l], R = slp[l + 1] - lo;
+    if (R >= RUN_WARPS) {
+      G = 1;
+      slot = warp;
+      sub = 0;
+    } else {
+      G = RUN_WARPS / R;
+      G = 1 << (31 - __clz(G));
+      slot = warp / G;
+      sub = warp % G;
+    }
+    step = 32 * G;
+    if (slot < R) {
+      const int t = lo + slot;
+      r = rows ? srw[t] : t;
+      q0 = srp[r] + sub * 32 + lane;
+      q1 = srp[r + 1];
+    } else {
+      r = -1;
+      q0 = q1 = 0;
+    }
+  };
+  int r = -1, q0 = 0, q1 = 0, step = 32, G = 1, slot = 0, sub = 0;
+  int pci = 0;
+  A pcv = A(0);
+  if (nlev > 0) {
+    assign(0, r, q0, q1, step, G, slot, sub);
+    if (q0 < q1) {
+      pci = ci[base + q0];
+      pcv = ld_arith(cv + base + q0);
+    }
+  }
   for (int l = 0; l < nlev; ++l) {
-    const int lo = lptr[l], hi = lptr[l + 1];
-    for (int t = lo + warp; t < hi; t += RUN_TPB / 32) {
-      const int r = rows ? rows[t] : t;
-      const int64_t b = rp[r], e = rp[r + 1];
-      A acc = A(0);
-      for (int64_t q = b + lane; q < e; q += 32) acc = fma_(ld_arith(cv + q), yt[ci[q]], acc);
-      acc = wsum(acc);
-      if (lane == 0) yt[r] = yt[r] - acc;
+    const int lo = slp[l], hi = slp[l + 1], R = hi - lo;
+    A acc = A(0);
+    if (q0 < q1) {
+      acc = pcv * yt[pci];
+      for (int q = q0 + step; q < q1; q += step) acc = fma_(ld_arith(cv + base + q), yt[ci[base + q]], acc);
+    }
+    acc = wsum(acc);
+    if (R >= RUN_WARPS) {
+      if (lane == 0 && r >= 0) yt[r] = yt[r] - acc;
+      for (int t = lo + warp + RUN_WARPS; t < hi; t += RUN_WARPS) {  // further rows of this warp
+        const int rr = rows ? srw[t] : t;
+        A a2 = A(0);
+        for (int q = srp[rr] + lane; q < srp[rr + 1]; q += 32) a2 = fma_(ld_arith(cv + base + q), yt[ci[base + q]], a2);
+        a2 = wsum(a2);
+        if (lane == 0) yt[rr] = yt[rr] - a2;
+      }
+    } else if (lane == 0) {
+      part[warp] = acc;
+    }
+    int nr = -1, nq0 = 0, nq1 = 0, nstep = 32, nG = 1, nslot = 0, nsub = 0;
+    if (l + 1 < nlev) {  // prefetch the first entry of the next level
+      assign(l + 1, nr, nq0, nq1, nstep, nG, nslot, nsub);
+      if (nq0 < nq1) {
+        pci = ci[base + nq0];
+        pcv = ld_arith(cv + base + nq0);
+      }
     }
     __syncthreads();
+    if (R < RUN_WARPS) {
+      if (slot < R && sub == 0 && lane == 0) {
+        A t = part[warp];
+        for (int j = 1; j < G; ++j) t = t + part[warp + j];
+        yt[r] = yt[r] - t;
+      }
+      __syncthreads();
+    }
+    r = nr; q0 = nq0; q1 = nq1; step = nstep; G = nG; slot = nslot; sub = nsub;
   }
   for (int t = threadIdx.x; t < m; t += RUN_TPB) y[s_tail + t] = yt[t];
 }
@@ -416,7 +519,8 @@ template <class T, class S> void ildl_apply(const DevFactor<S>& F, bool spd, con
     }
   };
   sweep(F.fseg, F.fptr, F.dfptr, nullptr, F.lp, F.li, F.lx);
-  const size_t tsm = sizeof(A) * (size_t)std::max(F.m_tail, 1);
+  const size_t tsm = std::max(tail_smem_bytes<A>(F.m_tail, (int)F.tfptr.size() - 1, false),
+                              tail_smem_bytes<A>(F.m_tail, (int)F.tbptr.size() - 1, true));
   ensure_tail_smem<S, A>(tsm);
   if (F.m_tail > 0) {
     const int nb = (F.m_tail + WIDE_TPB / WIDE_LANES - 1) / (WIDE_TPB / WIDE_LANES);
@@ -436,7 +540,9 @@ template <class T, class S> void ildl_apply_graph(DevFactor<S>& F, bool spd, con
   const int n = F.n;
   const int g = spd ? 1 : 0;
   if (!F.graph[g]) {
-    ensure_tail_smem<S, typename Arith<S>::type>(sizeof(typename Arith<S>::type) * (size_t)std::max(F.m_tail, 1));
+    using A = typename Arith<S>::type;
+    ensure_tail_smem<S, A>(std::max(tail_smem_bytes<A>(F.m_tail, (int)F.tfptr.size() - 1, false),
+                                    tail_smem_bytes<A>(F.m_tail, (int)F.tbptr.size() - 1, true)));
     cudaGraph_t gr;
     CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     ildl_apply<T, S>(F, spd, (const T*)F.rhs_in, (T*)F.sol_out, s);

@@ -641,12 +641,15 @@ struct OrcFactorD { jdg::IldlcFactor<double> F; };
 void orc_set_depth_weight(double w) { orc::g_depth_weight = w; }
 static double g_dropS = -1;
 void orc_set_drop_schur(double v) { g_dropS = v; }
+static int g_threads = 0;
+void orc_set_threads(int t) { g_threads = t; }
 void* orc_dfactor(int n, const int* ia, const int* ja, const double* a, double shift, double droptol, double condest,
                   double mem, int* ierr) {
   auto* h = new OrcFactorD;
   jdg::IldlcParams p;
   p.depth_weight = orc::g_depth_weight;
   p.droptol_schur = g_dropS;
+  p.threads = g_threads;
   p.droptol = droptol;
   p.condest = condest;
   p.mem = mem;
