@@ -151,6 +151,24 @@ JDG_API int jdgpu_dfactor_export(int* n_out, long long* nnz_out, double* shift_o
                                  double* lx, signed char* blk, double* dinv, double* doff, double* ainv,
                                  double* aoff);
 
+/* jdgpu_dildl_apply without allocating GPU memory.  No counterpart in the
+ * reference.  For callers that cannot call cudaMalloc: applications whose GPU
+ * memory is owned by another allocator (a framework's caching pool that must
+ * see every byte) or that fix their device-memory budget at start-up and
+ * treat any later allocation as an error.  The factor, the staging vectors
+ * and the work vector live in one fixed 32 MiB device array compiled into
+ * this library (every GPU that loads it keeps those 32 MiB until the process
+ * exits); problems that do not fit are rejected with -98 before any kernel
+ * runs.  Nothing in the array has to start at zero: each call writes every
+ * byte it later reads.  The first call on a device looks the array's address
+ * up (cudaGetSymbolAddress), so make that first call before any stream
+ * capture.  All calls share the one array: calls that overlap on the GPU race
+ * and must not be issued.  Arguments, results and other error codes as
+ * jdgpu_dildl_apply. */
+JDG_API int jdgpu_dildl_apply_noalloc(int n, const int* ia, const int* ja, const double* a, double shift,
+                                      double droptol, double condest, int spd, int precision, int nrhs,
+                                      const double* b, double* x, long* info);
+
 /* Options: "depth_weight" (ordering key weight of the triangular-solve
  * depth, default 2), "verbose". */
 JDG_API void jdgpu_set_option(const char* name, double value);

@@ -120,7 +120,18 @@ template <class S> void free_factor(DevFactor<S>& F) {
   F = DevFactor<S>();
 }
 
-template <class S, class H> void upload_factor(const IldlcFactor<H>& F, DevFactor<S>& D, cudaStream_t st) {
+// device memory for the factor arrays: cudaMalloc unless the caller supplies
+// another source
+struct DeviceMalloc {
+  void* operator()(size_t bytes) const {
+    void* p = nullptr;
+    CK(cudaMalloc(&p, bytes));
+    return p;
+  }
+};
+
+template <class S, class H, class Alloc = DeviceMalloc>
+void upload_factor(const IldlcFactor<H>& F, DevFactor<S>& D, cudaStream_t st, Alloc alloc = Alloc()) {
   free_factor(D);
   const int n = F.n;
   // forward levels over elimination steps; solve numbering s = level order
@@ -276,7 +287,7 @@ template <class S, class H> void upload_factor(const IldlcFactor<H>& F, DevFacto
   auto up_ = [&](auto*& dst, const auto& src) {
     using E = typename std::remove_reference<decltype(src)>::type::value_type;
     size_t bytes = sizeof(E) * std::max<size_t>(1, src.size());
-    CK(cudaMalloc((void**)&dst, bytes));
+    dst = (std::remove_reference_t<decltype(dst)>)alloc(bytes);
     if (!src.empty()) CK(cudaMemcpyAsync(dst, src.data(), sizeof(E) * src.size(), cudaMemcpyHostToDevice, st));
   };
   up_(D.orig, orig);
@@ -307,9 +318,9 @@ template <class S, class H> void upload_factor(const IldlcFactor<H>& F, DevFacto
   up_(D.tbv, tbv);
   up_(D.dtbptr, tbptr);
   up_(D.tbrows, tbrows);
-  CK(cudaMalloc(&D.y, sizeof(A) * std::max(1, n)));
-  CK(cudaMalloc(&D.rhs_in, sizeof(zc) * std::max(1, n)));
-  CK(cudaMalloc(&D.sol_out, sizeof(zc) * std::max(1, n)));
+  D.y = (A*)alloc(sizeof(A) * std::max(1, n));
+  D.rhs_in = alloc(sizeof(zc) * std::max(1, n));
+  D.sol_out = alloc(sizeof(zc) * std::max(1, n));
   k::ildl_plan(D, lp, up, brs);
   k::ildl_plan_bwd0(D);
   CK(cudaStreamSynchronize(st));
@@ -1041,6 +1052,49 @@ template <class S> static double precond_bytes(const DevFactor<S>& F) {
          8.0 * n * sv;
 }
 
+// ---------------------------------------------------- no-allocation path ----
+// Device storage of jdgpu_dildl_apply_noalloc: a fixed array in the
+// library's device image, present on every GPU that loads the library until
+// the process exits.  All calls share it; each call overwrites what it reads.
+constexpr size_t kNoallocScratchBytes = size_t(32) << 20;  // 32 MiB
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];
+
+// Host code cannot use g_noalloc_scratch as a pointer (it names the host-side
+// stand-in); the device address is looked up once per device, with that
+// device current.
+static void* noalloc_scratch_ptr() {
+  static std::mutex mu;
+  static void* ptrs[64] = {nullptr};
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) throw std::runtime_error("device index out of range");
+  std::lock_guard<std::mutex> lk(mu);
+  if (!ptrs[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+      throw std::runtime_error(std::string("cudaGetSymbolAddress of the scratch array failed: ") +
+                               cudaGetErrorString(e));
+    ptrs[dev] = p;
+  }
+  return ptrs[dev];
+}
+
+struct ScratchFull : std::runtime_error {
+  ScratchFull() : std::runtime_error("problem needs more device memory than the 32 MiB scratch array") {}
+};
+// hands out 256-byte aligned slices of the scratch array
+struct ScratchBump {
+  unsigned char* base;
+  size_t* used;
+  void* operator()(size_t bytes) const {
+    size_t off = (*used + 255) & ~size_t(255);
+    if (off > kNoallocScratchBytes || bytes > kNoallocScratchBytes - off) throw ScratchFull();
+    *used = off + bytes;
+    return base + off;
+  }
+};
+
 static void report(const std::exception& e, int* info) {
   std::fprintf(stderr, " JADAMILU-GB300 error: %s\n", e.what());
   *info = -54330;
@@ -1536,6 +1590,62 @@ JDG_API int jdgpu_dfactor_export(int* n_out, long long* nnz_out, double* shift_o
   std::copy(F.ainv.begin(), F.ainv.end(), ainv);
   std::copy(F.aoff.begin(), F.aoff.end(), aoff);
   return 0;
+}
+
+// The preconditioner application of jdgpu_dildl_apply without any GPU
+// memory allocation (see the header).  Returns 0, a factorisation error code,
+// -98 when the problem does not fit in the scratch array, -99 on a CUDA error.
+JDG_API int jdgpu_dildl_apply_noalloc(int n, const int* ia, const int* ja, const double* a, double shift,
+                                      double droptol, double condest, int spd, int precision, int nrhs,
+                                      const double* b, double* x, long* info) {
+  if (n <= 0 || nrhs < 0 || precision < 0 || precision > 2) return -1;
+  try {
+    unsigned char* base = (unsigned char*)noalloc_scratch_ptr();
+    IldlcParams p;
+    p.droptol = droptol;
+    p.condest = condest;
+    p.mem = 0;
+    p.depth_weight = g_opt.depth_weight;
+    IldlcFactor<double> F;
+    int ierr = ildlc_factor<double>(n, ia, ja, a, shift, nullptr, nullptr, nullptr, p, F);
+    if (ierr) return ierr;
+    cudaStream_t st = nullptr;
+    size_t used = 0;
+    ScratchBump bump{base, &used};
+    double* db = (double*)bump(sizeof(double) * n);
+    double* dx = (double*)bump(sizeof(double) * n);
+    DevFactor<double> Fd;
+    DevFactor<float> Fs;
+    DevFactor<__nv_bfloat16> Fb;
+    if (precision == 1) upload_factor(F, Fs, st, bump);
+    else if (precision == 2) upload_factor(F, Fb, st, bump);
+    else upload_factor(F, Fd, st, bump);
+    for (int r = 0; r < nrhs; ++r) {
+      CK(cudaMemcpy(db, b + (size_t)r * n, sizeof(double) * n, cudaMemcpyHostToDevice));
+      if (precision == 1) k::ildl_apply<double, float>(Fs, spd != 0, db, dx, st);
+      else if (precision == 2) k::ildl_apply<double, __nv_bfloat16>(Fb, spd != 0, db, dx, st);
+      else k::ildl_apply<double, double>(Fd, spd != 0, db, dx, st);
+      CK(cudaGetLastError());
+      CK(cudaMemcpy(x + (size_t)r * n, dx, sizeof(double) * n, cudaMemcpyDeviceToHost));
+    }
+    if (info) {
+      info[0] = (long)F.li.size();
+      info[1] = F.nneg;
+      info[2] = (long)F.level_start.size() - 1;
+      std::vector<int> fp, fr, bp, br;
+      ildlc_levels(F, fp, fr, bp, br);
+      info[3] = (long)fp.size() - 1;
+      info[4] = (long)bp.size() - 1;
+    }
+    // the DevFactor objects point into the scratch array: nothing to free
+    return 0;
+  } catch (ScratchFull& e) {
+    std::fprintf(stderr, "jdgpu_dildl_apply_noalloc: %s\n", e.what());
+    return -98;
+  } catch (std::exception& e) {
+    std::fprintf(stderr, "jdgpu_dildl_apply_noalloc: %s\n", e.what());
+    return -99;
+  }
 }
 
 JDG_API void jdgpu_set_option(const char* name, double value) {
