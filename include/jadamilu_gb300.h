@@ -122,8 +122,9 @@ JDG_API int jdgpu_dildl_apply(int n, const int* ia, const int* ja, const double*
 
 /* Time `reps` GPU applications of the factor of A - shift*I (inputs resident
  * on the device, CUDA events).  out (8): ms per application, nnz(L),
- * forward depth, backward depth, launches per application, factor seconds,
- * rows solved by the single-CTA tail kernels, unused. */
+ * forward depth, backward depth, kernels per application, factor seconds,
+ * rows of the tail (dense inverse or single-CTA levels), upload seconds
+ * (includes the tail inverse). */
 JDG_API int jdgpu_dildl_bench(int n, const int* ia, const int* ja, const double* a, double shift, double droptol,
                               double condest, int spd, int precision, int reps, double* out);
 
@@ -170,7 +171,13 @@ JDG_API int jdgpu_dildl_apply_noalloc(int n, const int* ia, const int* ja, const
                                       const double* b, double* x, long* info);
 
 /* Options: "depth_weight" (ordering key weight of the triangular-solve
- * depth, default 2), "verbose". */
+ * depth, default 64), "verbose", "dense_tail" (1: solve the deepest levels of
+ * the preconditioner with the explicit inverse of their block, default; 0:
+ * level by level in one CTA), "dense_max" (most rows of that block, default
+ * 32768), "drop_schur" (drop tolerance of the Schur-complement fill; negative:
+ * DROPTOL/10), "apply_graph" (1: jdgpu_dildl_apply replays the captured CUDA
+ * graph of the application, as the eigensolver does).  They apply to factors
+ * computed after the call. */
 JDG_API void jdgpu_set_option(const char* name, double value);
 
 /* Statistics of the last real solve (10 doubles): factor seconds, upload

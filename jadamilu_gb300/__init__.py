@@ -313,7 +313,7 @@ def ildl_bench(A, shift=0.0, droptol=1e-3, condest=5.0, spd=False, precision=0, 
                             reps, _p(out))
     if r != 0:
         raise RuntimeError(f"ildl bench failed ({r})")
-    keys = ["ms", "nnz_l", "fwd_depth", "bwd_depth", "launches", "factor_s", "tail_rows"]
+    keys = ["ms", "nnz_l", "fwd_depth", "bwd_depth", "launches", "factor_s", "tail_rows", "upload_s"]
     return dict(zip(keys, out.tolist()))
 
 

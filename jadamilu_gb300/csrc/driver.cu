@@ -20,6 +20,7 @@
 
 #include "devjd.cuh"
 #include "ildlc.hpp"
+#include "tail_inverse.hpp"
 #include "../../include/jadamilu_gb300.h"
 
 namespace jdg {
@@ -112,12 +113,50 @@ template <> struct StoreOf<bc> {
 template <class S> void free_factor(DevFactor<S>& F) {
   void* ps[] = {F.orig, F.lp,  F.li,  F.lx,  F.up,  F.ui,  F.ux,    F.brows, F.blk,   F.partner, F.dv,
                 F.dof,  F.av,  F.aof, F.y,   F.dfptr, F.dbptr, F.rhs_in, F.sol_out, F.tep, F.tei, F.tev,
-                F.tip,  F.tii, F.tiv, F.dtfptr, F.tbp, F.tbi, F.tbv, F.dtbptr, F.tbrows};
+                F.tip,  F.tii, F.tiv, F.dtfptr, F.tbp, F.tbi, F.tbv, F.dtbptr, F.tbrows,
+                F.tf,   F.tb,  F.itf, F.itb, F.irf, F.irb, F.part};
   for (void* p : ps)
     if (p) cudaFree(p);
   for (auto& g : F.graph)
     if (g) cudaGraphExecDestroy(g);
   F = DevFactor<S>();
+}
+
+struct Options {
+  double depth_weight = 64.0;
+  int verbose = 0;
+  int dense_tail = 1;          // solve the deepest levels with their explicit inverse
+  int dense_max = 32768;       // at most this many rows in the dense tail
+  double drop_schur = -1.0;    // IldlcParams::droptol_schur (negative: its default rule)
+  int apply_graph = 0;         // jdgpu_dildl_apply through the captured graph
+};
+static Options g_opt;
+
+// Where the dense tail starts: the level Lt that minimises the modelled time
+// of one application, 2 sweeps x (Lt level steps + one pass over the tail's
+// inverse tiles).  Level steps are latency-bound (a launch, or a barrier and a
+// dependent load inside a single-CTA run); the tile pass is bandwidth-bound.
+// Shallow factors keep the level path (returns nfl): below a saving of
+// min_saving per application, building and uploading the tiles costs more
+// than a solve gains, and substitution order keeps the rounding of the
+// sequential algorithm.
+static int choose_dense_tail(const std::vector<int>& fptr, int nfl, size_t elem_bytes, int dense_max) {
+  const double t_level = 2.5e-6, bw = 5.0e12, t_fixed = 12e-6, min_saving = 100e-6;
+  const int n = fptr[nfl];
+  double best = 2.0 * nfl * t_level;
+  int best_lt = nfl;
+  for (int lt = nfl - 1; lt >= 1; --lt) {
+    const int m = n - fptr[lt];
+    if (m > dense_max) break;
+    const double nt = (m + kTile - 1) / kTile;
+    const double bytes = 2.0 * nt * (nt + 1) / 2 * kTileElems * elem_bytes;
+    const double t = 2.0 * lt * t_level + bytes / bw + t_fixed;
+    if (t < best) {
+      best = t;
+      best_lt = lt;
+    }
+  }
+  return 2.0 * nfl * t_level - best >= min_saving ? best_lt : nfl;
 }
 
 // device memory for the factor arrays: cudaMalloc unless the caller supplies
@@ -160,12 +199,17 @@ void upload_factor(const IldlcFactor<H>& F, DevFactor<S>& D, cudaStream_t st, Al
   using A = typename DevFactor<S>::A;
   // per tail row: its y entry, a row pointer, a level pointer and a row index
   const int tail_max = std::min<int>(16384, (int)((200 * 1024) / (sizeof(A) + 12)));
+  const bool dense = g_opt.dense_tail != 0 && n > 0;
   int Lt = nfl, acc_rows = 0;
-  while (Lt > 1) {
-    int r = fptr[Lt] - fptr[Lt - 1];
-    if (r > 2048 || acc_rows + r > tail_max) break;
-    acc_rows += r;
-    --Lt;
+  if (dense) {
+    Lt = choose_dense_tail(fptr, nfl, sizeof(S), g_opt.dense_max);
+  } else {
+    while (Lt > 1) {
+      int r = fptr[Lt] - fptr[Lt - 1];
+      if (r > 2048 || acc_rows + r > tail_max) break;
+      acc_rows += r;
+      --Lt;
+    }
   }
   const int s_tail = fptr[Lt];
   const int m_tail = n - s_tail;
@@ -221,6 +265,26 @@ void upload_factor(const IldlcFactor<H>& F, DevFactor<S>& D, cudaStream_t st, Al
   }
   std::vector<int> tfptr;
   for (int l = Lt; l <= nfl; ++l) tfptr.push_back(fptr[l] - s_tail);
+  // dense tail: explicit inverse of the tail's diagonal block, from the
+  // internal entries in host precision
+  std::vector<S> tiles_f, tiles_b;
+  TileItems itf, itb;
+  const int nt = dense && m_tail > 0 ? (m_tail + kTile - 1) / kTile : 0;
+  if (nt > 0) {
+    std::vector<H> tih(tip[m_tail]);
+    for (int t = 0; t < m_tail; ++t) {
+      int s = s_tail + t;
+      int64_t oi = tip[t];
+      for (int64_t q = lp[s]; q < lp[s + 1]; ++q)
+        if (li[q] >= s_tail) tih[oi++] = lxh[q];
+    }
+    const int nth = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    tail_inverse<H, S>(m_tail, tip, tii, tih, tiles_f, tiles_b, nth, [](const H& v) { return StoreOf<S>::f(v); });
+    const int64_t ntiles = (int64_t)nt * (nt + 1) / 2;
+    const int chunk = (int)std::max<int64_t>(1, std::min<int64_t>(16, ntiles / (152 * 8)));
+    itf = make_items(nt, true, chunk);
+    itb = make_items(nt, false, chunk);
+  }
   // backward: tail rows first (all their dependents are tail rows), then the
   // bulk rows level by level (dependencies on tail rows are already final)
   std::vector<int> blev(n, 0);
@@ -318,6 +382,22 @@ void upload_factor(const IldlcFactor<H>& F, DevFactor<S>& D, cudaStream_t st, Al
   up_(D.tbv, tbv);
   up_(D.dtbptr, tbptr);
   up_(D.tbrows, tbrows);
+  // entries the level sweeps read: all of L and L^H on the level path; the
+  // bulk rows of both plus the tail's external entries with a dense tail
+  D.sweep_entries = nt > 0 ? lp[s_tail] + up[s_tail] + tep[m_tail] : 2 * lp[n];
+  D.tile_bytes = 2.0 * (double)tiles_f.size() * sizeof(S);
+  if (nt > 0) {
+    D.nt = nt;
+    up_(D.tf, tiles_f);
+    up_(D.tb, tiles_b);
+    up_(D.itf, itf.item);
+    up_(D.itb, itb.item);
+    up_(D.irf, itf.irow);
+    up_(D.irb, itb.irow);
+    D.nitf = (int)(itf.item.size() / 4);
+    D.nitb = (int)(itb.item.size() / 4);
+    D.part = (A*)alloc(sizeof(A) * 64 * (size_t)std::max(D.nitf, D.nitb));
+  }
   D.y = (A*)alloc(sizeof(A) * std::max(1, n));
   D.rhs_in = alloc(sizeof(zc) * std::max(1, n));
   D.sol_out = alloc(sizeof(zc) * std::max(1, n));
@@ -330,11 +410,6 @@ template <class T> struct LowOf { using type = float; using bf = __nv_bfloat16; 
 template <> struct LowOf<zc> { using type = cc; using bf = bc; };
 
 // ------------------------------------------------------- global state ----
-struct Options {
-  double depth_weight = 64.0;
-  int verbose = 0;
-};
-static Options g_opt;
 
 template <class T> struct Global {
   using H = typename HostOf<T>::type;
@@ -543,6 +618,7 @@ int pjdinit(Global<T>& g, Printer& P, int n, typename HostOf<T>::type* a, int* j
     prm.condest = condest;
     prm.mem = MEM;
     prm.depth_weight = g_opt.depth_weight;
+    prm.droptol_schur = g_opt.drop_schur;
     double tf0 = wall();
     int ierr = ildlc_factor<H>(n, ia, ja, a, g.shift0, gep ? ib : nullptr, gep ? jb : nullptr, gep ? b : nullptr,
                                prm, g.F);
@@ -1046,10 +1122,12 @@ std::function<void(long, long)> revcom_precond(Revcom& rc, typename HostOf<T>::t
 // and column indices, row pointers, the permutation and level lists, the
 // block-diagonal D, the input/output vectors (float64) and one read and one
 // write of the work vector per phase (gather, two sweeps, D, scatter).
+// With a dense tail the swept entries are the bulk rows' and the tail's
+// external ones, and both tile sets are read once per application.
 template <class S> static double precond_bytes(const DevFactor<S>& F) {
   const double n = F.n, sz = sizeof(S), sv = sizeof(typename DevFactor<S>::A);
-  return 2.0 * F.nnz_l * (sz + 4) + 2.0 * (n + 1) * 8 + 3.0 * n * 4 + n * (1 + 4 + 2 * sz) + 2.0 * n * 8 +
-         8.0 * n * sv;
+  return (double)F.sweep_entries * (sz + 4) + 2.0 * (n + 1) * 8 + 3.0 * n * 4 + n * (1 + 4 + 2 * sz) +
+         2.0 * n * 8 + 8.0 * n * sv + F.tile_bytes;
 }
 
 // ---------------------------------------------------- no-allocation path ----
@@ -1334,6 +1412,7 @@ JDG_API int jdgpu_dildl_apply(int n, const int* ia, const int* ja, const double*
     p.condest = condest;
     p.mem = 0;
     p.depth_weight = g_opt.depth_weight;
+    p.droptol_schur = g_opt.drop_schur;
     IldlcFactor<double> F;
     int ierr = ildlc_factor<double>(n, ia, ja, a, shift, nullptr, nullptr, nullptr, p, F);
     if (ierr) return ierr;
@@ -1344,17 +1423,29 @@ JDG_API int jdgpu_dildl_apply(int n, const int* ia, const int* ja, const double*
     DevFactor<double> Fd;
     DevFactor<float> Fs;
     DevFactor<__nv_bfloat16> Fb;
+    // with the "apply_graph" option the application goes through the captured
+    // graph on a stream of its own, as inside the eigensolver
+    const bool graph = g_opt.apply_graph != 0;
+    if (graph) CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
     if (precision == 1) upload_factor(F, Fs, st);
     else if (precision == 2) upload_factor(F, Fb, st);
     else upload_factor(F, Fd, st);
     for (int r = 0; r < nrhs; ++r) {
       CK(cudaMemcpy(db, b + (size_t)r * n, sizeof(double) * n, cudaMemcpyHostToDevice));
-      if (precision == 1) k::ildl_apply<double, float>(Fs, spd != 0, db, dx, st);
-      else if (precision == 2) k::ildl_apply<double, __nv_bfloat16>(Fb, spd != 0, db, dx, st);
-      else k::ildl_apply<double, double>(Fd, spd != 0, db, dx, st);
+      if (graph) {
+        if (precision == 1) k::ildl_apply_graph<double, float>(Fs, spd != 0, db, dx, st);
+        else if (precision == 2) k::ildl_apply_graph<double, __nv_bfloat16>(Fb, spd != 0, db, dx, st);
+        else k::ildl_apply_graph<double, double>(Fd, spd != 0, db, dx, st);
+        CK(cudaStreamSynchronize(st));
+      } else {
+        if (precision == 1) k::ildl_apply<double, float>(Fs, spd != 0, db, dx, st);
+        else if (precision == 2) k::ildl_apply<double, __nv_bfloat16>(Fb, spd != 0, db, dx, st);
+        else k::ildl_apply<double, double>(Fd, spd != 0, db, dx, st);
+      }
       CK(cudaGetLastError());
       CK(cudaMemcpy(x + (size_t)r * n, dx, sizeof(double) * n, cudaMemcpyDeviceToHost));
     }
+    if (graph) CK(cudaStreamDestroy(st));
     if (info) {
       info[0] = (long)F.li.size();
       info[1] = F.nneg;
@@ -1388,6 +1479,7 @@ JDG_API int jdgpu_dildl_bench(int n, const int* ia, const int* ja, const double*
     p.condest = condest;
     p.mem = 0;
     p.depth_weight = g_opt.depth_weight;
+    p.droptol_schur = g_opt.drop_schur;
     IldlcFactor<double> F;
     double t0 = wall();
     int ierr = ildlc_factor<double>(n, ia, ja, a, shift, nullptr, nullptr, nullptr, p, F);
@@ -1408,9 +1500,11 @@ JDG_API int jdgpu_dildl_bench(int n, const int* ia, const int* ja, const double*
       else if (precision == 2) k::ildl_apply_graph<double, __nv_bfloat16>(Fb, spd != 0, db, dx, st);
       else k::ildl_apply_graph<double, double>(Fd, spd != 0, db, dx, st);
     };
+    const double tu0 = wall();
     if (precision == 1) upload_factor(F, Fs, st);
     else if (precision == 2) upload_factor(F, Fb, st);
     else upload_factor(F, Fd, st);
+    const double tu = wall() - tu0;
     for (int r = 0; r < 3; ++r) run();
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
@@ -1422,11 +1516,9 @@ JDG_API int jdgpu_dildl_bench(int n, const int* ia, const int* ja, const double*
     CK(cudaEventSynchronize(e1));
     float ms = 0;
     CK(cudaEventElapsedTime(&ms, e0, e1));
-    const auto& seg = precision == 1 ? Fs.fseg : precision == 2 ? Fb.fseg : Fd.fseg;
-    const auto& segb = precision == 1 ? Fs.bseg : precision == 2 ? Fb.bseg : Fd.bseg;
-    long launches = 3;
-    for (size_t q = 0; q < seg.size(); q += 3) launches += seg[q + 2] ? 1 : 1;
-    for (size_t q = 0; q < segb.size(); q += 3) launches += 1;
+    const int g = spd != 0 ? 1 : 0;
+    const long long launches = precision == 1 ? Fs.graph_kernels[g] : precision == 2 ? Fb.graph_kernels[g]
+                                                                                     : Fd.graph_kernels[g];
     out[0] = ms / reps;
     out[1] = (double)F.li.size();
     {
@@ -1435,9 +1527,10 @@ JDG_API int jdgpu_dildl_bench(int n, const int* ia, const int* ja, const double*
       out[2] = (double)fp.size() - 1;
       out[3] = (double)bp.size() - 1;
     }
-    out[4] = (double)(launches + 3);
+    out[4] = (double)launches;
     out[6] = precision == 1 ? Fs.m_tail : precision == 2 ? Fb.m_tail : Fd.m_tail;
     out[5] = tf;
+    out[7] = tu;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     free_factor(Fd);
@@ -1606,6 +1699,7 @@ JDG_API int jdgpu_dildl_apply_noalloc(int n, const int* ia, const int* ja, const
     p.condest = condest;
     p.mem = 0;
     p.depth_weight = g_opt.depth_weight;
+    p.droptol_schur = g_opt.drop_schur;
     IldlcFactor<double> F;
     int ierr = ildlc_factor<double>(n, ia, ja, a, shift, nullptr, nullptr, nullptr, p, F);
     if (ierr) return ierr;
@@ -1650,6 +1744,10 @@ JDG_API int jdgpu_dildl_apply_noalloc(int n, const int* ia, const int* ja, const
 
 JDG_API void jdgpu_set_option(const char* name, double value) {
   if (!std::strcmp(name, "depth_weight")) g_opt.depth_weight = value;
+  else if (!std::strcmp(name, "dense_tail")) g_opt.dense_tail = (int)value;
+  else if (!std::strcmp(name, "dense_max")) g_opt.dense_max = (int)value;
+  else if (!std::strcmp(name, "drop_schur")) g_opt.drop_schur = value;
+  else if (!std::strcmp(name, "apply_graph")) g_opt.apply_graph = (int)value;
   else if (!std::strcmp(name, "verbose")) g_opt.verbose = (int)value;
 }
 

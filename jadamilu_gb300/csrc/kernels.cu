@@ -442,6 +442,68 @@ __global__ void __launch_bounds__(RUN_TPB) tail_run_kernel(int m, int s_tail, in
   for (int t = threadIdx.x; t < m; t += RUN_TPB) y[s_tail + t] = yt[t];
 }
 
+// Dense tail product  out = T x  over a set of 64 x 64 tiles (column-major
+// inside a tile).  One CTA per work item {tile row, first tile, tile count,
+// first tile column}: the item's slice of x goes to shared memory, every
+// thread streams 16-byte vectors of V consecutive rows of one tile column,
+// and the per-column partial sums are added in a fixed order, so results do
+// not depend on timing.  tri_reduce_kernel adds the items of each tile row
+// (in order) and writes the result.
+constexpr int TRI_TPB = 256, TRI_CH = 16;
+template <class S, class A>
+__global__ void __launch_bounds__(TRI_TPB) tri_partial_kernel(const int4* __restrict__ items,
+                                                             const S* __restrict__ tiles, const A* __restrict__ x,
+                                                             int m, A* __restrict__ part) {
+  constexpr int V = 16 / sizeof(S);   // elements per 16-byte vector
+  constexpr int RG = 64 / V;          // vectors per tile column
+  constexpr int CPS = TRI_TPB / RG;   // tile columns covered by one pass of the CTA
+  constexpr int NS = 64 / CPS;        // passes per tile
+  __shared__ A xs[TRI_CH * 64];
+  __shared__ A red[CPS][64];
+  const int4 it = items[blockIdx.x];
+  const int cnt = it.z, col0 = it.w * 64;
+  for (int t = threadIdx.x; t < cnt * 64; t += TRI_TPB) {
+    const int c = col0 + t;
+    xs[t] = c < m ? x[c] : A(0);
+  }
+  __syncthreads();
+  const int rg = threadIdx.x % RG, cs = threadIdx.x / RG;
+  A acc[V];
+#pragma unroll
+  for (int v = 0; v < V; ++v) acc[v] = A(0);
+  const uint4* tp = reinterpret_cast<const uint4*>(tiles) + (size_t)it.y * (64 * 64 / V);
+  for (int k = 0; k < cnt; ++k) {
+    uint4 buf[NS];
+#pragma unroll
+    for (int sl = 0; sl < NS; ++sl) buf[sl] = __ldg(tp + (size_t)k * (64 * 64 / V) + (sl * CPS + cs) * RG + rg);
+#pragma unroll
+    for (int sl = 0; sl < NS; ++sl) {
+      const A xv = xs[k * 64 + sl * CPS + cs];
+      const S* e = reinterpret_cast<const S*>(&buf[sl]);
+#pragma unroll
+      for (int v = 0; v < V; ++v) acc[v] = fma_(ld_arith(e + v), xv, acc[v]);
+    }
+  }
+#pragma unroll
+  for (int v = 0; v < V; ++v) red[cs][V * rg + v] = acc[v];
+  __syncthreads();
+  if (threadIdx.x < 64) {
+    A sum = red[0][threadIdx.x];
+#pragma unroll
+    for (int j = 1; j < CPS; ++j) sum = sum + red[j][threadIdx.x];
+    part[(size_t)blockIdx.x * 64 + threadIdx.x] = sum;
+  }
+}
+template <class A>
+__global__ void tri_reduce_kernel(int m, const int* __restrict__ irow, const A* __restrict__ part, A* __restrict__ y) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= m) return;
+  const int i = e >> 6, r = e & 63;
+  A sum = A(0);
+  for (int q = irow[i]; q < irow[i + 1]; ++q) sum = sum + part[(size_t)q * 64 + r];
+  y[e] = sum;
+}
+
 // raise the dynamic shared-memory limit of the tail kernel once per size
 // (done before any graph capture: ildl_apply_graph calls it first)
 template <class S, class A> static void ensure_tail_smem(size_t bytes) {
@@ -452,6 +514,8 @@ template <class S, class A> static void ensure_tail_smem(size_t bytes) {
   }
 }
 
+constexpr int kRunRows = 2 * RUN_WARPS;
+constexpr int64_t kRunEntries = 16384;
 template <class S>
 void ildl_plan(DevFactor<S>& F, const std::vector<int64_t>& lp, const std::vector<int64_t>& up,
                const std::vector<int>& brows) {
@@ -468,9 +532,12 @@ void ildl_plan(DevFactor<S>& F, const std::vector<int64_t>& lp, const std::vecto
         }
         return nz;
       };
+      // a level goes to the single-CTA run when each of its 32 warps has at
+      // most two rows (one dependent load round each); wider levels are one
+      // grid launch, whose cost does not grow with the row count
       int rows = ptr[l + 1] - ptr[l];
       int64_t nz = work(l);
-      bool narrow = rows <= 2048 && nz <= 65536;
+      bool narrow = rows <= kRunRows && nz <= kRunEntries;
       if (!narrow) {
         seg.insert(seg.end(), {l, l + 1, 0});
         ++l;
@@ -479,7 +546,7 @@ void ildl_plan(DevFactor<S>& F, const std::vector<int64_t>& lp, const std::vecto
       int l1 = l + 1;
       while (l1 < nl) {
         int r = ptr[l1 + 1] - ptr[l1];
-        if (r > 2048 || work(l1) > 65536) break;
+        if (r > kRunRows || work(l1) > kRunEntries) break;
         ++l1;
       }
       seg.insert(seg.end(), {l, l1, 1});
@@ -519,19 +586,31 @@ template <class T, class S> void ildl_apply(const DevFactor<S>& F, bool spd, con
     }
   };
   sweep(F.fseg, F.fptr, F.dfptr, nullptr, F.lp, F.li, F.lx);
-  const size_t tsm = std::max(tail_smem_bytes<A>(F.m_tail, (int)F.tfptr.size() - 1, false),
-                              tail_smem_bytes<A>(F.m_tail, (int)F.tbptr.size() - 1, true));
-  ensure_tail_smem<S, A>(tsm);
+  const bool dense = F.nt > 0, levels = F.m_tail > 0 && !dense;
+  const size_t tsm = levels ? std::max(tail_smem_bytes<A>(F.m_tail, (int)F.tfptr.size() - 1, false),
+                                       tail_smem_bytes<A>(F.m_tail, (int)F.tbptr.size() - 1, true))
+                            : 0;
+  if (levels) ensure_tail_smem<S, A>(tsm);
+  A* yt = F.y + F.s_tail;
   if (F.m_tail > 0) {
     const int nb = (F.m_tail + WIDE_TPB / WIDE_LANES - 1) / (WIDE_TPB / WIDE_LANES);
     tail_ext_kernel<S, A><<<nb, WIDE_TPB, 0, s>>>(F.m_tail, F.s_tail, F.tep, F.tei, F.tev, F.y);
+  }
+  if (dense) {
+    tri_partial_kernel<S, A><<<F.nitf, TRI_TPB, 0, s>>>((const int4*)F.itf, F.tf, yt, F.m_tail, F.part);
+    tri_reduce_kernel<A><<<nblk(F.m_tail), TPB, 0, s>>>(F.m_tail, F.irf, F.part, yt);
+  } else if (levels) {
     tail_run_kernel<S, A><<<1, RUN_TPB, tsm, s>>>(F.m_tail, F.s_tail, (int)F.tfptr.size() - 1, F.dtfptr, nullptr,
                                                  F.tip, F.tii, F.tiv, F.y);
   }
   ildl_dsolve_kernel<S, A><<<nblk(n), TPB, 0, s>>>(n, F.blk, F.partner, spd ? F.av : F.dv, spd ? F.aof : F.dof, F.y);
-  if (F.m_tail > 0)
+  if (dense) {
+    tri_partial_kernel<S, A><<<F.nitb, TRI_TPB, 0, s>>>((const int4*)F.itb, F.tb, yt, F.m_tail, F.part);
+    tri_reduce_kernel<A><<<nblk(F.m_tail), TPB, 0, s>>>(F.m_tail, F.irb, F.part, yt);
+  } else if (levels) {
     tail_run_kernel<S, A><<<1, RUN_TPB, tsm, s>>>(F.m_tail, F.s_tail, (int)F.tbptr.size() - 1, F.dtbptr, F.tbrows,
                                                  F.tbp, F.tbi, F.tbv, F.y);
+  }
   sweep(F.bseg, F.bptr, F.dbptr, F.brows, F.up, F.ui, F.ux);
   ildl_scatter_kernel<T, A><<<nblk(n), TPB, 0, s>>>(n, F.orig, F.y, x);
 }
@@ -541,8 +620,9 @@ template <class T, class S> void ildl_apply_graph(DevFactor<S>& F, bool spd, con
   const int g = spd ? 1 : 0;
   if (!F.graph[g]) {
     using A = typename Arith<S>::type;
-    ensure_tail_smem<S, A>(std::max(tail_smem_bytes<A>(F.m_tail, (int)F.tfptr.size() - 1, false),
-                                    tail_smem_bytes<A>(F.m_tail, (int)F.tbptr.size() - 1, true)));
+    if (F.m_tail > 0 && F.nt == 0)
+      ensure_tail_smem<S, A>(std::max(tail_smem_bytes<A>(F.m_tail, (int)F.tfptr.size() - 1, false),
+                                      tail_smem_bytes<A>(F.m_tail, (int)F.tbptr.size() - 1, true)));
     cudaGraph_t gr;
     CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     ildl_apply<T, S>(F, spd, (const T*)F.rhs_in, (T*)F.sol_out, s);

@@ -51,6 +51,18 @@ template <class S> struct DevFactor {
   int* dtfptr = nullptr; std::vector<int> tfptr;                  // forward tail levels (local rows)
   int64_t* tbp = nullptr; int* tbi = nullptr; S* tbv = nullptr;   // backward tail rows of L^H (local)
   int* dtbptr = nullptr; int* tbrows = nullptr; std::vector<int> tbptr;
+  // Dense tail: when nt > 0 the rows s >= s_tail are solved with the
+  // explicit inverse of their diagonal block, nt x nt tiles of 64 x 64
+  // (forward set tf = Linv, backward set tb = Linv^H; layout in
+  // tail_inverse.hpp), after the external entries (tep/tei/tev) are applied.
+  int nt = 0;
+  S* tf = nullptr; S* tb = nullptr;
+  int* itf = nullptr; int* itb = nullptr;    // work items, 4 ints each
+  int nitf = 0, nitb = 0;
+  int* irf = nullptr; int* irb = nullptr;    // items of each tile row
+  A* part = nullptr;                         // per-item partial sums (64 each)
+  int64_t sweep_entries = 0;                 // L / L^H entries the two level sweeps read
+  double tile_bytes = 0;                     // bytes of both tile sets
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   long long graph_kernels[2] = {0, 0};
   void* rhs_in = nullptr;

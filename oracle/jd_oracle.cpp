@@ -30,6 +30,7 @@ namespace orc {
 
 // ordering weight of the triangular-solve depth (same default as the GPU library)
 static double g_depth_weight = 64.0;
+static double g_drop_schur = -1.0;  // IldlcParams::droptol_schur (negative: its default rule)
 
 static double now_s() {
   using namespace std::chrono;
@@ -262,6 +263,7 @@ int pjdinit(Global<T>& g, int n, T* a, int* ja, int* ia, const T* b, const int* 
     const double nposeig = (icntl[2] <= 0) ? 0.01 : 0.0;
     jdg::IldlcParams prm;
     prm.depth_weight = g_depth_weight;
+    prm.droptol_schur = g_drop_schur;
     prm.droptol = DROPTOL;
     prm.condest = condest;
     prm.mem = MEM;
@@ -639,8 +641,7 @@ void orc_zmatveca(int n, const int* ia, const int* ja, const cplx* a, const cplx
 // opaque handle, for kernel-level parity of the GPU preconditioner.
 struct OrcFactorD { jdg::IldlcFactor<double> F; };
 void orc_set_depth_weight(double w) { orc::g_depth_weight = w; }
-static double g_dropS = -1;
-void orc_set_drop_schur(double v) { g_dropS = v; }
+void orc_set_drop_schur(double v) { orc::g_drop_schur = v; }
 static int g_threads = 0;
 void orc_set_threads(int t) { g_threads = t; }
 void* orc_dfactor(int n, const int* ia, const int* ja, const double* a, double shift, double droptol, double condest,
@@ -648,7 +649,7 @@ void* orc_dfactor(int n, const int* ia, const int* ja, const double* a, double s
   auto* h = new OrcFactorD;
   jdg::IldlcParams p;
   p.depth_weight = orc::g_depth_weight;
-  p.droptol_schur = g_dropS;
+  p.droptol_schur = orc::g_drop_schur;
   p.threads = g_threads;
   p.droptol = droptol;
   p.condest = condest;
