@@ -170,6 +170,20 @@ JDG_API int jdgpu_dildl_apply_noalloc(int n, const int* ia, const int* ja, const
                                       double droptol, double condest, int spd, int precision, int nrhs,
                                       const double* b, double* x, long* info);
 
+/* Gradient of f = sum_k w[k] * lambda_k with respect to every stored entry
+ * of A, for eigenpairs of A x = lambda B x (B = I, or B diagonal with its
+ * diagonal in bdiag; NULL for B = I).  ia/ja: the one-triangle CSR of A as
+ * passed to DPJD / DPJD_GEP (1-based; the order DPJD leaves the entries in
+ * is fine).  X: the eigenvectors, n x neig column-major with leading
+ * dimension ldx (DPJD's X), any scaling.  grad[q] for stored entry q (i, j):
+ * sum_k w_k x_k(i) x_k(j) / (x_k^T B x_k), doubled off the diagonal since the
+ * entry stands for a_ij and a_ji (Hellmann-Feynman; B held fixed).  For a
+ * cluster of equal eigenvalues give the whole cluster one weight.  An
+ * extension with no counterpart in the reference.  neig <= 64.  Returns 0,
+ * -1 on bad arguments, -99 on a CUDA error. */
+JDG_API int jdgpu_deig_grad(int n, const int* ia, const int* ja, int neig, const double* X, int ldx,
+                            const double* w, const double* bdiag, double* grad);
+
 /* Options: "depth_weight" (ordering key weight of the triangular-solve
  * depth, default 64), "verbose", "dense_tail" (1: solve the deepest levels of
  * the preconditioner with the explicit inverse of their block, default; 0:

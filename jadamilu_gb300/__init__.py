@@ -64,6 +64,7 @@ def load(build_if_missing: bool = True):
     L.jdgpu_dildl_apply.argtypes = [C.c_int, _P, _P, _P, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int,
                                     C.c_int, _P, _P, _P]
     L.jdgpu_set_option.argtypes = [C.c_char_p, C.c_double]
+    L.jdgpu_deig_grad.argtypes = [C.c_int, _P, _P, C.c_int, _P, C.c_int, _P, _P, _P]
     L.jdgpu_dildl_bench.argtypes = [C.c_int, _P, _P, _P, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int,
                                     C.c_int, _P]
     L.jdgpu_dprepare_matrix.argtypes = [C.c_int, _P, _P, _P]
@@ -285,6 +286,25 @@ def ildl_apply(A, b, shift=0.0, droptol=1e-3, condest=5.0, spd=False, precision=
         raise RuntimeError(f"GPU ILDL apply failed ({r})")
     keys = ["nnz_l", "nneg", "nlevels", "fwd_depth", "bwd_depth"]
     return X.reshape(b.shape), dict(zip(keys, info.tolist()))
+
+
+def eig_grad(A, X, w=None, bdiag=None):
+    """Gradient of sum_k w[k] * lambda_k with respect to the stored entries of
+    A = (a, ja, ia), from eigenvectors X (n x k, columns; any scaling) of
+    A x = lambda B x with B = diag(bdiag) or I (jdgpu_deig_grad)."""
+    L = load()
+    _require_gpu(L)
+    a, ja, ia = _matrix(A, np.float64)
+    n = len(ia) - 1
+    X = np.asfortranarray(np.asarray(X, np.float64).reshape(n, -1))
+    k = X.shape[1]
+    w = np.ones(k) if w is None else np.ascontiguousarray(w, np.float64)
+    bd = None if bdiag is None else np.ascontiguousarray(bdiag, np.float64)
+    g = np.zeros(len(a))
+    r = L.jdgpu_deig_grad(n, _p(ia), _p(ja), k, _p(X), n, _p(w), _p(bd) if bd is not None else None, _p(g))
+    if r != 0:
+        raise RuntimeError(f"jdgpu_deig_grad failed ({r})")
+    return g
 
 
 def set_option(name: str, value: float) -> None:

@@ -25,7 +25,7 @@ ORACLE_LIB = os.path.join(ORACLE_DIR, "_build", "liboracle.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hidden", "--expt-relaxed-constexpr",
            "-I" + os.path.join(ROOT, "include")]
-UNITS = ["kernels.cu", "devjd.cu", "driver.cu"]
+UNITS = ["kernels.cu", "devjd.cu", "driver.cu", "grad.cu"]
 
 
 def _nvcc():

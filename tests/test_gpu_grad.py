@@ -1,0 +1,64 @@
+"""Eigenvalue gradients (jdgpu_deig_grad) on the P1-FEM generalized problem
+K x = lambda M x: against the Hellmann-Feynman formula evaluated in numpy,
+and against central finite differences of the eigenvalue sum (the
+differentiation configuration's check, at a reduced grid)."""
+import numpy as np
+import pytest
+
+from jadamilu_gb300 import matrices as M
+
+pytestmark = pytest.mark.gpu
+
+
+def _rows_cols(ia, ja):
+    n = len(ia) - 1
+    return np.repeat(np.arange(n), np.diff(ia)), np.asarray(ja) - 1
+
+
+def test_eig_grad_matches_formula_any_scaling(gpu):
+    import scipy.linalg as sl
+    K, Mm = M.fem_p1(20, seed=3)
+    ia, ja, a = K
+    Kd = M.to_scipy_full(*K).toarray()
+    md = M.to_scipy_full(*Mm).toarray().diagonal()
+    w, X = sl.eigh(Kd, np.diag(md))
+    X = X[:, :6]
+    rows, cols = _rows_cols(ia, ja)
+    wts = np.array([1.0, 0.5, 2.0, 1.0, -1.0, 3.0])
+    ref = np.sum(wts * X[rows] * X[cols], 1) * np.where(rows == cols, 1.0, 2.0)
+    # the entry point normalises by x^T M x, so scaled eigenvectors give the same gradient
+    scale = np.array([1.0, -3.0, 0.25, 7.0, 1e-3, 2.0])
+    g = gpu.eig_grad((a, ja, ia), X * scale, w=wts, bdiag=md)
+    np.testing.assert_allclose(g, ref, rtol=1e-12, atol=1e-12 * np.abs(ref).max())
+
+
+def test_eig_grad_of_gpu_eigenpairs_matches_central_differences(gpu):
+    """Gradient of the sum of the 6 smallest eigenvalues from the GPU solver's
+    eigenvectors, against central differences on 40 seeded stored entries.
+    Step 1e-6 (the configuration's step): the differences carry rounding of
+    about eps*|f|/h, so the bound is 1e-5 of max|g|; step 1e-4: 1e-6."""
+    import scipy.linalg as sl
+    K, Mm = M.fem_p1(20, seed=3)
+    r = gpu.dpjd_gep((K[2], K[1], K[0]), (Mm[2], Mm[1], Mm[0]), 6, isearch=0, madspace=20, maxit=4000,
+                     tol=1e-10, droptol=1e-3)
+    assert r["info"] == 0 and r["neig"] == 6
+    a, ja, ia = r["a"], r["ja"], r["ia"]
+    md = M.to_scipy_full(*Mm).toarray().diagonal()
+    g = gpu.eig_grad((a, ja, ia), r["x"][:, :6], bdiag=md)
+    Kd = M.to_scipy_full(ia, ja, a).toarray()
+    rows, cols = _rows_cols(ia, ja)
+    qs = np.random.default_rng(7).choice(len(a), 40, replace=False)
+    for h, bound in ((1e-6, 1e-5), (1e-4, 1e-6)):
+        fd = np.empty(len(qs))
+        for t, q in enumerate(qs):
+            i, j = rows[q], cols[q]
+            f = []
+            for sgn in (1.0, -1.0):
+                Kp = Kd.copy()
+                Kp[i, j] += sgn * h
+                if i != j:
+                    Kp[j, i] += sgn * h
+                f.append(np.sum(sl.eigh(Kp, np.diag(md), eigvals_only=True)[:6]))
+            fd[t] = (f[0] - f[1]) / (2 * h)
+        err = np.max(np.abs(fd - g[qs])) / np.max(np.abs(g))
+        assert err <= bound, (h, err)
