@@ -114,9 +114,14 @@ template <class S> void free_factor(DevFactor<S>& F) {
   void* ps[] = {F.orig, F.lp,  F.li,  F.lx,  F.up,  F.ui,  F.ux,    F.brows, F.blk,   F.partner, F.dv,
                 F.dof,  F.av,  F.aof, F.y,   F.dfptr, F.dbptr, F.rhs_in, F.sol_out, F.tep, F.tei, F.tev,
                 F.tip,  F.tii, F.tiv, F.dtfptr, F.tbp, F.tbi, F.tbv, F.dtbptr, F.tbrows,
-                F.tf,   F.tb,  F.itf, F.itb, F.irf, F.irb, F.part};
+                F.part};
   for (void* p : ps)
     if (p) cudaFree(p);
+  for (auto& B : F.blocks) {
+    void* bs[] = {B.ep, B.ei, B.ev, B.bp, B.bi, B.bv, B.tf, B.tb, B.itf, B.itb, B.irf, B.irb};
+    for (void* p : bs)
+      if (p) cudaFree(p);
+  }
   for (auto& g : F.graph)
     if (g) cudaGraphExecDestroy(g);
   F = DevFactor<S>();
@@ -132,31 +137,65 @@ struct Options {
 };
 static Options g_opt;
 
-// Where the dense tail starts: the level Lt that minimises the modelled time
-// of one application, 2 sweeps x (Lt level steps + one pass over the tail's
-// inverse tiles).  Level steps are latency-bound (a launch, or a barrier and a
-// dependent load inside a single-CTA run); the tile pass is bandwidth-bound.
-// Shallow factors keep the level path (returns nfl): below a saving of
-// min_saving per application, building and uploading the tiles costs more
-// than a solve gains, and substitution order keeps the rounding of the
+// Blocks after the bulk levels.  Each group {a, b, dense} covers forward
+// levels [a, b); dense groups are solved with the explicit inverse of their
+// diagonal block, the others are single levels.  The plan minimises a model
+// of one application (both sweeps): a level costs one launch per sweep plus
+// its entries' bytes; a dense block costs three launches per sweep (external
+// entries, tile product, reduction) plus its external entries and both tile
+// sets.  Levels before the first dense block stay on the bulk level path.
+// Shallow factors keep the level path entirely (empty plan): below a saving
+// of min_saving per application, building and uploading the tiles costs
+// more than a solve gains, and substitution order keeps the rounding of the
 // sequential algorithm.
-static int choose_dense_tail(const std::vector<int>& fptr, int nfl, size_t elem_bytes, int dense_max) {
-  const double t_level = 2.5e-6, bw = 5.0e12, t_fixed = 12e-6, min_saving = 100e-6;
-  const int n = fptr[nfl];
-  double best = 2.0 * nfl * t_level;
-  int best_lt = nfl;
-  for (int lt = nfl - 1; lt >= 1; --lt) {
-    const int m = n - fptr[lt];
-    if (m > dense_max) break;
-    const double nt = (m + kTile - 1) / kTile;
-    const double bytes = 2.0 * nt * (nt + 1) / 2 * kTileElems * elem_bytes;
-    const double t = 2.0 * lt * t_level + bytes / bw + t_fixed;
-    if (t < best) {
-      best = t;
-      best_lt = lt;
+struct BlockGroup {
+  int a, b;
+  bool dense;
+};
+static std::vector<BlockGroup> plan_dense_blocks(const std::vector<int>& fptr, const std::vector<int64_t>& ent_f,
+                                                 const std::vector<int64_t>& ent_b, size_t elem_bytes, int dense_max) {
+  const int nfl = (int)fptr.size() - 1;
+  const double t_launch = 4e-6, bw = 5.0e12, min_saving = 100e-6;
+  const double eb = (double)elem_bytes + 4;
+  auto c_lev = [&](int l) { return (l > 0 ? 2 : 1) * t_launch + (double)(ent_f[l] + ent_b[l]) * eb / bw; };
+  std::vector<double> best(nfl + 1, 0.0);
+  std::vector<int> nxt(nfl + 1, -1);
+  for (int a = nfl - 1; a >= 0; --a) {
+    best[a] = c_lev(a) + best[a + 1];
+    if (a == 0) continue;
+    double ent = 0;
+    for (int b = a + 1; b <= nfl; ++b) {
+      const int m = fptr[b] - fptr[a];
+      if (m > dense_max) break;
+      ent += (double)(ent_f[b - 1] + ent_b[b - 1]);
+      const double nt = (m + kTile - 1) / kTile;
+      const double c = 6 * t_launch + 2.0 * nt * (nt + 1) / 2 * kTileElems * elem_bytes / bw + ent * eb / bw;
+      if (c + best[b] < best[a]) {
+        best[a] = c + best[b];
+        nxt[a] = b;
+      }
     }
   }
-  return 2.0 * nfl * t_level - best >= min_saving ? best_lt : nfl;
+  double all_levels = 0;
+  for (int l = 0; l < nfl; ++l) all_levels += c_lev(l);
+  std::vector<BlockGroup> g;
+  int first = -1;
+  for (int a = 1; a < nfl; ++a)
+    if (nxt[a] >= 0) {
+      first = a;
+      break;
+    }
+  if (first < 0 || all_levels - best[0] < min_saving) return g;
+  for (int a = first; a < nfl;) {
+    if (nxt[a] >= 0) {
+      g.push_back({a, nxt[a], true});
+      a = nxt[a];
+    } else {
+      g.push_back({a, a + 1, false});
+      ++a;
+    }
+  }
+  return g;
 }
 
 // device memory for the factor arrays: cudaMalloc unless the caller supplies
@@ -199,20 +238,6 @@ void upload_factor(const IldlcFactor<H>& F, DevFactor<S>& D, cudaStream_t st, Al
   using A = typename DevFactor<S>::A;
   // per tail row: its y entry, a row pointer, a level pointer and a row index
   const int tail_max = std::min<int>(16384, (int)((200 * 1024) / (sizeof(A) + 12)));
-  const bool dense = g_opt.dense_tail != 0 && n > 0;
-  int Lt = nfl, acc_rows = 0;
-  if (dense) {
-    Lt = choose_dense_tail(fptr, nfl, sizeof(S), g_opt.dense_max);
-  } else {
-    while (Lt > 1) {
-      int r = fptr[Lt] - fptr[Lt - 1];
-      if (r > 2048 || acc_rows + r > tail_max) break;
-      acc_rows += r;
-      --Lt;
-    }
-  }
-  const int s_tail = fptr[Lt];
-  const int m_tail = n - s_tail;
   // forward rows in s numbering
   std::vector<int> orig(n);
   std::vector<int64_t> lp(n + 1, 0);
@@ -244,18 +269,46 @@ void upload_factor(const IldlcFactor<H>& F, DevFactor<S>& D, cudaStream_t st, Al
         ux[fu[c]++] = StoreOf<S>::f(jdd::cj(lxh[q]));
       }
   }
+  // rows from s_tail on: dense blocks (plan_dense_blocks), or with the
+  // dense_tail option off the deepest run of narrow levels in one CTA
+  const bool dense_opt = g_opt.dense_tail != 0 && n > 0;
+  std::vector<BlockGroup> groups;
+  int Lt = nfl;
+  if (dense_opt) {
+    std::vector<int64_t> ent_f(nfl, 0), ent_b(nfl, 0);
+    for (int l = 0; l < nfl; ++l)
+      for (int s = fptr[l]; s < fptr[l + 1]; ++s) {
+        ent_f[l] += lp[s + 1] - lp[s];
+        ent_b[l] += up[s + 1] - up[s];
+      }
+    groups = plan_dense_blocks(fptr, ent_f, ent_b, sizeof(S), g_opt.dense_max);
+    if (!groups.empty()) Lt = groups[0].a;
+  } else {
+    int acc_rows = 0;
+    while (Lt > 1) {
+      int r = fptr[Lt] - fptr[Lt - 1];
+      if (r > 2048 || acc_rows + r > tail_max) break;
+      acc_rows += r;
+      --Lt;
+    }
+  }
+  const bool dense = !groups.empty();
+  const int s_tail = fptr[Lt];
+  const int m_tail = n - s_tail;
+  // the single-CTA tail arrays (level path only; empty with dense blocks)
+  const int m_lv = dense ? 0 : m_tail;
   // forward tail split into external / internal entries
-  std::vector<int64_t> tep(m_tail + 1, 0), tip(m_tail + 1, 0);
-  for (int t = 0; t < m_tail; ++t) {
+  std::vector<int64_t> tep(m_lv + 1, 0), tip(m_lv + 1, 0);
+  for (int t = 0; t < m_lv; ++t) {
     int s = s_tail + t;
     int64_t ne = 0, ni = 0;
     for (int64_t q = lp[s]; q < lp[s + 1]; ++q) (li[q] < s_tail ? ne : ni)++;
     tep[t + 1] = tep[t] + ne;
     tip[t + 1] = tip[t] + ni;
   }
-  std::vector<int> tei(tep[m_tail]), tii(tip[m_tail]);
-  std::vector<S> tev(tep[m_tail]), tiv(tip[m_tail]);
-  for (int t = 0; t < m_tail; ++t) {
+  std::vector<int> tei(tep[m_lv]), tii(tip[m_lv]);
+  std::vector<S> tev(tep[m_lv]), tiv(tip[m_lv]);
+  for (int t = 0; t < m_lv; ++t) {
     int s = s_tail + t;
     int64_t oe = tep[t], oi = tip[t];
     for (int64_t q = lp[s]; q < lp[s + 1]; ++q) {
@@ -265,26 +318,6 @@ void upload_factor(const IldlcFactor<H>& F, DevFactor<S>& D, cudaStream_t st, Al
   }
   std::vector<int> tfptr;
   for (int l = Lt; l <= nfl; ++l) tfptr.push_back(fptr[l] - s_tail);
-  // dense tail: explicit inverse of the tail's diagonal block, from the
-  // internal entries in host precision
-  std::vector<S> tiles_f, tiles_b;
-  TileItems itf, itb;
-  const int nt = dense && m_tail > 0 ? (m_tail + kTile - 1) / kTile : 0;
-  if (nt > 0) {
-    std::vector<H> tih(tip[m_tail]);
-    for (int t = 0; t < m_tail; ++t) {
-      int s = s_tail + t;
-      int64_t oi = tip[t];
-      for (int64_t q = lp[s]; q < lp[s + 1]; ++q)
-        if (li[q] >= s_tail) tih[oi++] = lxh[q];
-    }
-    const int nth = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
-    tail_inverse<H, S>(m_tail, tip, tii, tih, tiles_f, tiles_b, nth, [](const H& v) { return StoreOf<S>::f(v); });
-    const int64_t ntiles = (int64_t)nt * (nt + 1) / 2;
-    const int chunk = (int)std::max<int64_t>(1, std::min<int64_t>(16, ntiles / (152 * 8)));
-    itf = make_items(nt, true, chunk);
-    itb = make_items(nt, false, chunk);
-  }
   // backward: tail rows first (all their dependents are tail rows), then the
   // bulk rows level by level (dependencies on tail rows are already final)
   std::vector<int> blev(n, 0);
@@ -307,18 +340,18 @@ void upload_factor(const IldlcFactor<H>& F, DevFactor<S>& D, cudaStream_t st, Al
     std::vector<int> f(bptr.begin(), bptr.end() - 1);
     for (int s = 0; s < s_tail; ++s) brs[f[blev[s]]++] = s;
   }
-  std::vector<int> tbptr(ntl + 1, 0), tbrows(m_tail);
-  for (int t = 0; t < m_tail; ++t) tbptr[blev[s_tail + t] + 1]++;
+  std::vector<int> tbptr(ntl + 1, 0), tbrows(m_lv);
+  for (int t = 0; t < m_lv; ++t) tbptr[blev[s_tail + t] + 1]++;
   for (int l = 0; l < ntl; ++l) tbptr[l + 1] += tbptr[l];
   {
     std::vector<int> f(tbptr.begin(), tbptr.end() - 1);
-    for (int t = 0; t < m_tail; ++t) tbrows[f[blev[s_tail + t]]++] = t;
+    for (int t = 0; t < m_lv; ++t) tbrows[f[blev[s_tail + t]]++] = t;
   }
-  std::vector<int64_t> tbp(m_tail + 1, 0);
-  for (int t = 0; t < m_tail; ++t) tbp[t + 1] = tbp[t] + (up[s_tail + t + 1] - up[s_tail + t]);
-  std::vector<int> tbi(tbp[m_tail]);
-  std::vector<S> tbv(tbp[m_tail]);
-  for (int t = 0; t < m_tail; ++t) {
+  std::vector<int64_t> tbp(m_lv + 1, 0);
+  for (int t = 0; t < m_lv; ++t) tbp[t + 1] = tbp[t] + (up[s_tail + t + 1] - up[s_tail + t]);
+  std::vector<int> tbi(tbp[m_lv]);
+  std::vector<S> tbv(tbp[m_lv]);
+  for (int t = 0; t < m_lv; ++t) {
     int64_t o = tbp[t];
     for (int64_t q = up[s_tail + t]; q < up[s_tail + t + 1]; ++q, ++o) {
       tbi[o] = ui[q] - s_tail;
@@ -382,22 +415,72 @@ void upload_factor(const IldlcFactor<H>& F, DevFactor<S>& D, cudaStream_t st, Al
   up_(D.tbv, tbv);
   up_(D.dtbptr, tbptr);
   up_(D.tbrows, tbrows);
-  // entries the level sweeps read: all of L and L^H on the level path; the
-  // bulk rows of both plus the tail's external entries with a dense tail
-  D.sweep_entries = nt > 0 ? lp[s_tail] + up[s_tail] + tep[m_tail] : 2 * lp[n];
-  D.tile_bytes = 2.0 * (double)tiles_f.size() * sizeof(S);
-  if (nt > 0) {
-    D.nt = nt;
-    up_(D.tf, tiles_f);
-    up_(D.tb, tiles_b);
-    up_(D.itf, itf.item);
-    up_(D.itb, itb.item);
-    up_(D.irf, itf.irow);
-    up_(D.irb, itb.irow);
-    D.nitf = (int)(itf.item.size() / 4);
-    D.nitb = (int)(itb.item.size() / 4);
-    D.part = (A*)alloc(sizeof(A) * 64 * (size_t)std::max(D.nitf, D.nitb));
+  // dense blocks: external entries of both sweeps and, for dense groups, the
+  // explicit inverse of the diagonal block from the internal entries in host
+  // precision; each block is uploaded as soon as it is built
+  D.sweep_entries = dense ? lp[s_tail] + up[s_tail] : 2 * lp[n];
+  D.tile_bytes = 0;
+  size_t max_items = 0;
+  const int nth = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  for (const auto& gr : groups) {
+    DenseBlk<S> B;
+    B.s0 = fptr[gr.a];
+    B.m = fptr[gr.b] - B.s0;
+    std::vector<int64_t> ep(B.m + 1, 0), bp(B.m + 1, 0), ip(B.m + 1, 0);
+    std::vector<int> ei, bi, ii;
+    std::vector<S> ev, bv;
+    std::vector<H> iv;
+    for (int t = 0; t < B.m; ++t) {
+      const int s = B.s0 + t;
+      for (int64_t q = lp[s]; q < lp[s + 1]; ++q) {
+        if (li[q] < B.s0) {
+          ei.push_back(li[q]);
+          ev.push_back(lx[q]);
+        } else {
+          ii.push_back(li[q] - B.s0);
+          iv.push_back(lxh[q]);
+        }
+      }
+      for (int64_t q = up[s]; q < up[s + 1]; ++q)
+        if (ui[q] >= B.s0 + B.m) {
+          bi.push_back(ui[q]);
+          bv.push_back(ux[q]);
+        }
+      ep[t + 1] = (int64_t)ei.size();
+      bp[t + 1] = (int64_t)bi.size();
+      ip[t + 1] = (int64_t)ii.size();
+    }
+    B.nfe = (int64_t)ei.size();
+    B.nbe = (int64_t)bi.size();
+    D.sweep_entries += B.nfe + B.nbe;
+    up_(B.ep, ep);
+    up_(B.ei, ei);
+    up_(B.ev, ev);
+    up_(B.bp, bp);
+    up_(B.bi, bi);
+    up_(B.bv, bv);
+    if (gr.dense) {
+      std::vector<S> tf, tb;
+      tail_inverse<H, S>(B.m, ip, ii, iv, tf, tb, nth, [](const H& v) { return StoreOf<S>::f(v); });
+      B.nt = (B.m + kTile - 1) / kTile;
+      const int64_t ntiles = (int64_t)B.nt * (B.nt + 1) / 2;
+      const int chunk = (int)std::max<int64_t>(1, std::min<int64_t>(16, ntiles / (152 * 8)));
+      TileItems itf = make_items(B.nt, true, chunk), itb = make_items(B.nt, false, chunk);
+      up_(B.tf, tf);
+      up_(B.tb, tb);
+      up_(B.itf, itf.item);
+      up_(B.itb, itb.item);
+      up_(B.irf, itf.irow);
+      up_(B.irb, itb.irow);
+      B.nitf = (int)(itf.item.size() / 4);
+      B.nitb = (int)(itb.item.size() / 4);
+      max_items = std::max(max_items, (size_t)std::max(B.nitf, B.nitb));
+      D.tile_bytes += 2.0 * (double)tf.size() * sizeof(S);
+    }
+    CK(cudaStreamSynchronize(st));  // the host vectors of this block are released next
+    D.blocks.push_back(B);
   }
+  if (max_items > 0) D.part = (A*)alloc(sizeof(A) * 64 * max_items);
   D.y = (A*)alloc(sizeof(A) * std::max(1, n));
   D.rhs_in = alloc(sizeof(zc) * std::max(1, n));
   D.sol_out = alloc(sizeof(zc) * std::max(1, n));

@@ -586,27 +586,40 @@ template <class T, class S> void ildl_apply(const DevFactor<S>& F, bool spd, con
     }
   };
   sweep(F.fseg, F.fptr, F.dfptr, nullptr, F.lp, F.li, F.lx);
-  const bool dense = F.nt > 0, levels = F.m_tail > 0 && !dense;
+  const bool dense = !F.blocks.empty(), levels = F.m_tail > 0 && !dense;
+  auto ext = [&](int m, int s0, const int64_t* rp, const int* ci, const S* cv) {
+    const int nb = (m + WIDE_TPB / WIDE_LANES - 1) / (WIDE_TPB / WIDE_LANES);
+    tail_ext_kernel<S, A><<<nb, WIDE_TPB, 0, s>>>(m, s0, rp, ci, cv, F.y);
+  };
   const size_t tsm = levels ? std::max(tail_smem_bytes<A>(F.m_tail, (int)F.tfptr.size() - 1, false),
                                        tail_smem_bytes<A>(F.m_tail, (int)F.tbptr.size() - 1, true))
                             : 0;
   if (levels) ensure_tail_smem<S, A>(tsm);
-  A* yt = F.y + F.s_tail;
-  if (F.m_tail > 0) {
-    const int nb = (F.m_tail + WIDE_TPB / WIDE_LANES - 1) / (WIDE_TPB / WIDE_LANES);
-    tail_ext_kernel<S, A><<<nb, WIDE_TPB, 0, s>>>(F.m_tail, F.s_tail, F.tep, F.tei, F.tev, F.y);
-  }
   if (dense) {
-    tri_partial_kernel<S, A><<<F.nitf, TRI_TPB, 0, s>>>((const int4*)F.itf, F.tf, yt, F.m_tail, F.part);
-    tri_reduce_kernel<A><<<nblk(F.m_tail), TPB, 0, s>>>(F.m_tail, F.irf, F.part, yt);
+    for (const auto& B : F.blocks) {
+      A* yb = F.y + B.s0;
+      if (B.nfe > 0) ext(B.m, B.s0, B.ep, B.ei, B.ev);
+      if (B.nt > 0) {
+        tri_partial_kernel<S, A><<<B.nitf, TRI_TPB, 0, s>>>((const int4*)B.itf, B.tf, yb, B.m, F.part);
+        tri_reduce_kernel<A><<<nblk(B.m), TPB, 0, s>>>(B.m, B.irf, F.part, yb);
+      }
+    }
   } else if (levels) {
+    ext(F.m_tail, F.s_tail, F.tep, F.tei, F.tev);
     tail_run_kernel<S, A><<<1, RUN_TPB, tsm, s>>>(F.m_tail, F.s_tail, (int)F.tfptr.size() - 1, F.dtfptr, nullptr,
                                                  F.tip, F.tii, F.tiv, F.y);
   }
   ildl_dsolve_kernel<S, A><<<nblk(n), TPB, 0, s>>>(n, F.blk, F.partner, spd ? F.av : F.dv, spd ? F.aof : F.dof, F.y);
   if (dense) {
-    tri_partial_kernel<S, A><<<F.nitb, TRI_TPB, 0, s>>>((const int4*)F.itb, F.tb, yt, F.m_tail, F.part);
-    tri_reduce_kernel<A><<<nblk(F.m_tail), TPB, 0, s>>>(F.m_tail, F.irb, F.part, yt);
+    for (auto it = F.blocks.rbegin(); it != F.blocks.rend(); ++it) {
+      const auto& B = *it;
+      A* yb = F.y + B.s0;
+      if (B.nbe > 0) ext(B.m, B.s0, B.bp, B.bi, B.bv);
+      if (B.nt > 0) {
+        tri_partial_kernel<S, A><<<B.nitb, TRI_TPB, 0, s>>>((const int4*)B.itb, B.tb, yb, B.m, F.part);
+        tri_reduce_kernel<A><<<nblk(B.m), TPB, 0, s>>>(B.m, B.irb, F.part, yb);
+      }
+    }
   } else if (levels) {
     tail_run_kernel<S, A><<<1, RUN_TPB, tsm, s>>>(F.m_tail, F.s_tail, (int)F.tbptr.size() - 1, F.dtbptr, F.tbrows,
                                                  F.tbp, F.tbi, F.tbv, F.y);
@@ -620,7 +633,7 @@ template <class T, class S> void ildl_apply_graph(DevFactor<S>& F, bool spd, con
   const int g = spd ? 1 : 0;
   if (!F.graph[g]) {
     using A = typename Arith<S>::type;
-    if (F.m_tail > 0 && F.nt == 0)
+    if (F.m_tail > 0 && F.blocks.empty())
       ensure_tail_smem<S, A>(std::max(tail_smem_bytes<A>(F.m_tail, (int)F.tfptr.size() - 1, false),
                                       tail_smem_bytes<A>(F.m_tail, (int)F.tbptr.size() - 1, true)));
     cudaGraph_t gr;

@@ -18,6 +18,23 @@ template <class T> struct SellMatrix {
   T* val = nullptr;
 };
 
+// A block of consecutive rows [s0, s0 + m) after the bulk levels.  Forward:
+// its external entries (columns < s0) are applied, then, when nt > 0, the
+// explicit inverse of its diagonal block as nt x nt tiles of 64 x 64 (layout
+// in tail_inverse.hpp).  Backward (blocks in reverse order): the entries of
+// L^H pointing past the block, then the tiles of the inverse's adjoint.  A
+// block with nt = 0 is one dependency level (identity diagonal block).
+template <class S> struct DenseBlk {
+  int s0 = 0, m = 0, nt = 0;
+  int64_t* ep = nullptr; int* ei = nullptr; S* ev = nullptr;   // forward external, rows local
+  int64_t* bp = nullptr; int* bi = nullptr; S* bv = nullptr;   // backward external (L^H), rows local
+  int64_t nfe = 0, nbe = 0;                                    // entry counts
+  S* tf = nullptr; S* tb = nullptr;                            // tiles of Linv and Linv^H
+  int* itf = nullptr; int* itb = nullptr;                      // work items, 4 ints each
+  int nitf = 0, nitb = 0;
+  int* irf = nullptr; int* irb = nullptr;                      // items of each tile row
+};
+
 // Level-scheduled factor on the device, in "solve numbering" s: rows of the
 // same forward level are contiguous; L^H rows are listed level by level in
 // brows.  S is the storage type, A = Arith<S>::type the arithmetic type.
@@ -51,15 +68,9 @@ template <class S> struct DevFactor {
   int* dtfptr = nullptr; std::vector<int> tfptr;                  // forward tail levels (local rows)
   int64_t* tbp = nullptr; int* tbi = nullptr; S* tbv = nullptr;   // backward tail rows of L^H (local)
   int* dtbptr = nullptr; int* tbrows = nullptr; std::vector<int> tbptr;
-  // Dense tail: when nt > 0 the rows s >= s_tail are solved with the
-  // explicit inverse of their diagonal block, nt x nt tiles of 64 x 64
-  // (forward set tf = Linv, backward set tb = Linv^H; layout in
-  // tail_inverse.hpp), after the external entries (tep/tei/tev) are applied.
-  int nt = 0;
-  S* tf = nullptr; S* tb = nullptr;
-  int* itf = nullptr; int* itb = nullptr;    // work items, 4 ints each
-  int nitf = 0, nitb = 0;
-  int* irf = nullptr; int* irb = nullptr;    // items of each tile row
+  // Dense blocks: when non-empty, the rows s >= s_tail are solved block by
+  // block (DenseBlk) instead of by the single-CTA tail kernels.
+  std::vector<DenseBlk<S>> blocks;
   A* part = nullptr;                         // per-item partial sums (64 each)
   int64_t sweep_entries = 0;                 // L / L^H entries the two level sweeps read
   double tile_bytes = 0;                     // bytes of both tile sets
