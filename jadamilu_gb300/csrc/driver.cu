@@ -485,7 +485,7 @@ void upload_factor(const IldlcFactor<H>& F, DevFactor<S>& D, cudaStream_t st, Al
   D.rhs_in = alloc(sizeof(zc) * std::max(1, n));
   D.sol_out = alloc(sizeof(zc) * std::max(1, n));
   k::ildl_plan(D, lp, up, brs);
-  k::ildl_plan_bwd0(D);
+  k::ildl_plan_bwd0(D, up, brs);
   CK(cudaStreamSynchronize(st));
 }
 

@@ -70,7 +70,14 @@ __device__ __forceinline__ cc shfl_xor_any(cc v, int o) { return cc(shfl_xor_any
 __device__ __forceinline__ zc shfl_xor_any(zc v, int o) { return zc(shfl_xor_any(v.x, o), shfl_xor_any(v.y, o)); }
 
 constexpr int MD_CH = 8;  // columns per pass
-static inline int md_grid(long n) { return (int)std::min<long>(std::max<long>(1, (n + 2047) / 2048), 152L * 4); }
+// Long vectors: up to two rows per thread, enough CTAs in flight to stream V
+// at full bandwidth.  Vectors under 4096 rows keep one CTA per 2048 rows, the
+// summation order validated on the user-guide samples (n = 1000), whose JD
+// trajectories change with the rounding of these inner products.
+static inline int md_grid(long n) {
+  if (n < 4096) return (int)std::max<long>(1, (n + 2047) / 2048);
+  return (int)std::min<long>((n + 511) / 512, 152L * 8);
+}
 long mdot_partial_size(long n, int k) { return (long)md_grid(n) * ((k + MD_CH - 1) / MD_CH) * MD_CH; }
 
 template <class T>
@@ -303,14 +310,18 @@ __global__ void __launch_bounds__(RUN_TPB) ildl_run_kernel(int l0, int l1, const
     }
   }
 }
-// One wide level: 8 lanes per row.
-constexpr int WIDE_TPB = 256, WIDE_LANES = 8;
-template <class S, class A>
+// One wide level: LANES lanes per row (8, 16 or 32, from the level's mean
+// row length, so long rows are read by more lanes at once).
+constexpr int WIDE_TPB = 256;
+static inline int lanes_for(double entries_per_row) {
+  return entries_per_row >= 48 ? 32 : entries_per_row >= 20 ? 16 : 8;
+}
+template <class S, class A, int LANES>
 __global__ void __launch_bounds__(WIDE_TPB) ildl_wide_kernel(int lo, int hi, const int* __restrict__ rows,
                                                             const int64_t* __restrict__ rp, const int* __restrict__ ci,
                                                             const S* __restrict__ cv, A* __restrict__ y) {
-  const int g = blockIdx.x * (WIDE_TPB / WIDE_LANES) + (threadIdx.x / WIDE_LANES);
-  const int lane = threadIdx.x % WIDE_LANES;
+  const int g = blockIdx.x * (WIDE_TPB / LANES) + (threadIdx.x / LANES);
+  const int lane = threadIdx.x % LANES;
   const int t = lo + g;
   const bool ok = t < hi;
   int s = 0;
@@ -318,24 +329,40 @@ __global__ void __launch_bounds__(WIDE_TPB) ildl_wide_kernel(int lo, int hi, con
   if (ok) {
     s = rows ? rows[t] : t;
     const int64_t b = rp[s], e = rp[s + 1];
-    for (int64_t q = b + lane; q < e; q += WIDE_LANES) acc = fma_(ld_arith(cv + q), y[ci[q]], acc);
+    for (int64_t q = b + lane; q < e; q += LANES) acc = fma_(ld_arith(cv + q), y[ci[q]], acc);
   }
-  for (int o = WIDE_LANES / 2; o > 0; o >>= 1) acc = acc + shfl_xor_any(acc, o);
+  for (int o = LANES / 2; o > 0; o >>= 1) acc = acc + shfl_xor_any(acc, o);
   if (ok && lane == 0) y[s] = y[s] - acc;
 }
 
-// Forward tail, external part: y[s] -= sum over entries with column < s_tail.
-template <class S, class A>
+// Rows [s0, s0 + m) of a block: y[s0 + t] -= sum of row t's entries (local
+// row pointers, global columns), LANES lanes per row.
+template <class S, class A, int LANES>
 __global__ void __launch_bounds__(WIDE_TPB) tail_ext_kernel(int m, int s_tail, const int64_t* __restrict__ rp,
                                                            const int* __restrict__ ci, const S* __restrict__ cv,
                                                            A* __restrict__ y) {
-  const int t = blockIdx.x * (WIDE_TPB / WIDE_LANES) + (threadIdx.x / WIDE_LANES);
-  const int lane = threadIdx.x % WIDE_LANES;
+  const int t = blockIdx.x * (WIDE_TPB / LANES) + (threadIdx.x / LANES);
+  const int lane = threadIdx.x % LANES;
   A acc = A(0);
   if (t < m)
-    for (int64_t q = rp[t] + lane; q < rp[t + 1]; q += WIDE_LANES) acc = fma_(ld_arith(cv + q), y[ci[q]], acc);
-  for (int o = WIDE_LANES / 2; o > 0; o >>= 1) acc = acc + shfl_xor_any(acc, o);
+    for (int64_t q = rp[t] + lane; q < rp[t + 1]; q += LANES) acc = fma_(ld_arith(cv + q), y[ci[q]], acc);
+  for (int o = LANES / 2; o > 0; o >>= 1) acc = acc + shfl_xor_any(acc, o);
   if (t < m && lane == 0) y[s_tail + t] = y[s_tail + t] - acc;
+}
+template <class S, class A>
+static void launch_wide(int lanes, int lo, int hi, const int* rows, const int64_t* rp, const int* ci, const S* cv, A* y,
+                        cudaStream_t s) {
+  const int nb = (hi - lo) * lanes / WIDE_TPB + 1;
+  if (lanes == 32) ildl_wide_kernel<S, A, 32><<<nb, WIDE_TPB, 0, s>>>(lo, hi, rows, rp, ci, cv, y);
+  else if (lanes == 16) ildl_wide_kernel<S, A, 16><<<nb, WIDE_TPB, 0, s>>>(lo, hi, rows, rp, ci, cv, y);
+  else ildl_wide_kernel<S, A, 8><<<nb, WIDE_TPB, 0, s>>>(lo, hi, rows, rp, ci, cv, y);
+}
+template <class S, class A>
+static void launch_ext(int lanes, int m, int s0, const int64_t* rp, const int* ci, const S* cv, A* y, cudaStream_t s) {
+  const int nb = m * lanes / WIDE_TPB + 1;
+  if (lanes == 32) tail_ext_kernel<S, A, 32><<<nb, WIDE_TPB, 0, s>>>(m, s0, rp, ci, cv, y);
+  else if (lanes == 16) tail_ext_kernel<S, A, 16><<<nb, WIDE_TPB, 0, s>>>(m, s0, rp, ci, cv, y);
+  else tail_ext_kernel<S, A, 8><<<nb, WIDE_TPB, 0, s>>>(m, s0, rp, ci, cv, y);
 }
 // The sequential part of a tail sweep in one CTA.  Shared memory holds the
 // tail of y (yt), the row pointers relative to the first tail entry, the level
@@ -539,7 +566,7 @@ void ildl_plan(DevFactor<S>& F, const std::vector<int64_t>& lp, const std::vecto
       int64_t nz = work(l);
       bool narrow = rows <= kRunRows && nz <= kRunEntries;
       if (!narrow) {
-        seg.insert(seg.end(), {l, l + 1, 0});
+        seg.insert(seg.end(), {l, l + 1, lanes_for((double)nz / std::max(1, rows))});
         ++l;
         continue;
       }
@@ -557,11 +584,13 @@ void ildl_plan(DevFactor<S>& F, const std::vector<int64_t>& lp, const std::vecto
   plan(F.bptr, false, F.bseg);
 }
 // levels of the bulk backward sweep start at 0 (rows may point into the tail)
-template <class S> void ildl_plan_bwd0(DevFactor<S>& F) {
+template <class S> void ildl_plan_bwd0(DevFactor<S>& F, const std::vector<int64_t>& up, const std::vector<int>& brows) {
   std::vector<int> seg;
   for (size_t q = 0; q < F.bseg.size(); q += 3) seg.insert(seg.end(), {F.bseg[q], F.bseg[q + 1], F.bseg[q + 2]});
   if (F.bptr.size() > 1 && (F.bseg.empty() || F.bseg[0] != 0)) {
-    std::vector<int> s0 = {0, 1, 0};
+    int64_t nz = 0;
+    for (int t = F.bptr[0]; t < F.bptr[1]; ++t) nz += up[brows[t] + 1] - up[brows[t]];
+    std::vector<int> s0 = {0, 1, lanes_for((double)nz / std::max(1, F.bptr[1] - F.bptr[0]))};
     s0.insert(s0.end(), seg.begin(), seg.end());
     seg = s0;
   }
@@ -579,17 +608,14 @@ template <class T, class S> void ildl_apply(const DevFactor<S>& F, bool spd, con
       if (seg[q + 2] == 1) {
         ildl_run_kernel<S, A><<<1, RUN_TPB, 0, s>>>(l0, l1, dptr, rows, rp, ci, cv, F.y);
       } else {
-        int lo = ptr[l0], hi = ptr[l0 + 1];
-        int nb = (hi - lo + WIDE_TPB / WIDE_LANES - 1) / (WIDE_TPB / WIDE_LANES);
-        ildl_wide_kernel<S, A><<<nb, WIDE_TPB, 0, s>>>(lo, hi, rows, rp, ci, cv, F.y);
+        launch_wide<S, A>(seg[q + 2], ptr[l0], ptr[l0 + 1], rows, rp, ci, cv, F.y, s);
       }
     }
   };
   sweep(F.fseg, F.fptr, F.dfptr, nullptr, F.lp, F.li, F.lx);
   const bool dense = !F.blocks.empty(), levels = F.m_tail > 0 && !dense;
-  auto ext = [&](int m, int s0, const int64_t* rp, const int* ci, const S* cv) {
-    const int nb = (m + WIDE_TPB / WIDE_LANES - 1) / (WIDE_TPB / WIDE_LANES);
-    tail_ext_kernel<S, A><<<nb, WIDE_TPB, 0, s>>>(m, s0, rp, ci, cv, F.y);
+  auto ext = [&](int m, int s0, const int64_t* rp, const int* ci, const S* cv, int64_t entries) {
+    launch_ext<S, A>(lanes_for((double)entries / std::max(1, m)), m, s0, rp, ci, cv, F.y, s);
   };
   const size_t tsm = levels ? std::max(tail_smem_bytes<A>(F.m_tail, (int)F.tfptr.size() - 1, false),
                                        tail_smem_bytes<A>(F.m_tail, (int)F.tbptr.size() - 1, true))
@@ -598,14 +624,14 @@ template <class T, class S> void ildl_apply(const DevFactor<S>& F, bool spd, con
   if (dense) {
     for (const auto& B : F.blocks) {
       A* yb = F.y + B.s0;
-      if (B.nfe > 0) ext(B.m, B.s0, B.ep, B.ei, B.ev);
+      if (B.nfe > 0) ext(B.m, B.s0, B.ep, B.ei, B.ev, B.nfe);
       if (B.nt > 0) {
         tri_partial_kernel<S, A><<<B.nitf, TRI_TPB, 0, s>>>((const int4*)B.itf, B.tf, yb, B.m, F.part);
         tri_reduce_kernel<A><<<nblk(B.m), TPB, 0, s>>>(B.m, B.irf, F.part, yb);
       }
     }
   } else if (levels) {
-    ext(F.m_tail, F.s_tail, F.tep, F.tei, F.tev);
+    ext(F.m_tail, F.s_tail, F.tep, F.tei, F.tev, 8 * (int64_t)F.m_tail);
     tail_run_kernel<S, A><<<1, RUN_TPB, tsm, s>>>(F.m_tail, F.s_tail, (int)F.tfptr.size() - 1, F.dtfptr, nullptr,
                                                  F.tip, F.tii, F.tiv, F.y);
   }
@@ -614,7 +640,7 @@ template <class T, class S> void ildl_apply(const DevFactor<S>& F, bool spd, con
     for (auto it = F.blocks.rbegin(); it != F.blocks.rend(); ++it) {
       const auto& B = *it;
       A* yb = F.y + B.s0;
-      if (B.nbe > 0) ext(B.m, B.s0, B.bp, B.bi, B.bv);
+      if (B.nbe > 0) ext(B.m, B.s0, B.bp, B.bi, B.bv, B.nbe);
       if (B.nt > 0) {
         tri_partial_kernel<S, A><<<B.nitb, TRI_TPB, 0, s>>>((const int4*)B.itb, B.tb, yb, B.m, F.part);
         tri_reduce_kernel<A><<<nblk(B.m), TPB, 0, s>>>(B.m, B.irb, F.part, yb);
@@ -670,7 +696,7 @@ JD_INST_T(zc)
   template void ildl_apply_graph<T, S>(DevFactor<S>&, bool, const T*, T*, cudaStream_t);          \
   template void ildl_plan<S>(DevFactor<S>&, const std::vector<int64_t>&, const std::vector<int64_t>&, \
                              const std::vector<int>&);                                          \
-  template void ildl_plan_bwd0<S>(DevFactor<S>&);
+  template void ildl_plan_bwd0<S>(DevFactor<S>&, const std::vector<int64_t>&, const std::vector<int>&);
 JD_INST_F(double, double)
 JD_INST_F(double, float)
 JD_INST_F(double, __nv_bfloat16)

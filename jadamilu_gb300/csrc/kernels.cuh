@@ -48,8 +48,9 @@ template <class S> struct DevFactor {
   int* brows = nullptr;
   std::vector<int> fptr, bptr;               // level boundaries (host)
   int* dfptr = nullptr; int* dbptr = nullptr; // the same on the device
-  // sweep segments: {first level, last level + 1, kind}; kind 0 = one grid
-  // launch per level, 1 = one single-CTA launch for the whole run of levels
+  // sweep segments: {first level, last level + 1, kind}; kind 1 = one
+  // single-CTA launch for the whole run of levels, 8/16/32 = one grid launch
+  // for one level with that many lanes per row
   std::vector<int> fseg, bseg;
   signed char* blk = nullptr; int* partner = nullptr;
   S *dv = nullptr, *dof = nullptr, *av = nullptr, *aof = nullptr;  // D^{-1} and |D|^{-1}
@@ -110,7 +111,8 @@ template <class T, class S> void ildl_apply_graph(DevFactor<S>& F, bool spd, con
 template <class S> void ildl_plan(DevFactor<S>& F, const std::vector<int64_t>& lp_host, const std::vector<int64_t>& up_host,
                                   const std::vector<int>& brows_host);
 // make the bulk backward sweep start at level 0 (its rows may point into the tail)
-template <class S> void ildl_plan_bwd0(DevFactor<S>& F);
+template <class S> void ildl_plan_bwd0(DevFactor<S>& F, const std::vector<int64_t>& up_host,
+                                      const std::vector<int>& brows_host);
 
 }  // namespace k
 }  // namespace jdg
