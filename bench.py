@@ -53,15 +53,31 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--size", type=int, default=DEFAULT_SIZE, help="lattice edge m (n = m^3; 100 is the named 1e6 case)")
+    ap.add_argument("--workload", default="anderson", choices=["anderson", "laplace", "tightbinding", "fem"],
+                    help="anderson: the headline 3-D Anderson model (default); laplace: 20^3 Dirichlet Laplacian, "
+                         "plain float64; tightbinding: complex Hermitian 64^3 Peierls model, complex64 factor; "
+                         "fem: P1-FEM K x = lambda M x, 512^2 nodes, float64")
+    ap.add_argument("--size", type=int, default=None,
+                    help="lattice edge m (anderson: n = m^3, default %d, 100 is the named 1e6 case; laplace 20; "
+                         "tightbinding 64; fem: nodes per side, 512)" % DEFAULT_SIZE)
     ap.add_argument("--droptol", type=float, default=3e-3)
     ap.add_argument("--mem", type=float, default=60.0)
-    ap.add_argument("--precision", type=int, default=1, help="ICNTL(5): 0 fp64, 1 fp32, 2 bf16 factor")
-    ap.add_argument("--neig", type=int, default=10)
+    ap.add_argument("--precision", type=int, default=None,
+                    help="ICNTL(5): 0 fp64, 1 fp32, 2 bf16 factor (default: 1 for anderson and tightbinding, 0 else)")
+    ap.add_argument("--neig", type=int, default=None, help="default: 10 (anderson, laplace), 8, 6")
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="budget of the CPU-baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
-    return ap.parse_args()
+    args = ap.parse_args()
+    defaults = {"anderson": (DEFAULT_SIZE, 1, 10), "laplace": (20, 0, 10), "tightbinding": (64, 1, 8),
+                "fem": (512, 0, 6)}[args.workload]
+    if args.size is None:
+        args.size = defaults[0]
+    if args.precision is None:
+        args.precision = defaults[1]
+    if args.neig is None:
+        args.neig = defaults[2]
+    return args
 
 
 def dist_env():
@@ -122,6 +138,19 @@ class Clocks:
                 "samples": len(sm)}
 
 
+def _finite(v):
+    """JSON-safe copy: NaN (a figure not measured for this workload) becomes null."""
+    if isinstance(v, dict):
+        return {k: _finite(x) for k, x in v.items()}
+    if isinstance(v, (list, tuple)):
+        return [_finite(x) for x in v]
+    if isinstance(v, (float, np.floating)) and not np.isfinite(v):
+        return None
+    if isinstance(v, np.floating):
+        return float(v)
+    return v
+
+
 def measured_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -131,18 +160,59 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
+def make_workload(args):
+    """Matrix and solver settings of the chosen workload (synthetic, seeded)."""
+    from jadamilu_gb300 import matrices as M
+    w = {"name": args.workload, "B": None, "kind": "d", "resident": True}
+    if args.workload == "anderson":
+        w["A"] = M.anderson3d(args.size, disorder=16.5, seed=0)
+        w["kw"] = dict(isearch=2, sigma=0.0, madspace=25, droptol=args.droptol, mem=args.mem)
+        w["desc"] = (f"anderson3d {args.size}^3 periodic, W=16.5, seed 0, n={args.size ** 3}, {args.neig} eigpairs "
+                     f"closest to 0, TOL 1e-10")
+    elif args.workload == "laplace":
+        w["A"] = M.laplace3d(args.size)
+        w["kw"] = dict(isearch=0, sigma=0.0, madspace=20, droptol=1e-3, mem=20.0)
+        w["desc"] = f"7-point Dirichlet Laplacian {args.size}^3, n={args.size ** 3}, {args.neig} smallest, TOL 1e-10"
+    elif args.workload == "tightbinding":
+        w["A"] = M.tight_binding3d(args.size, phi=1.0 / 17.0, disorder=4.0, seed=1)
+        w["kw"] = dict(isearch=0, sigma=0.0, madspace=20, droptol=1e-3, mem=20.0)
+        w["kind"], w["resident"] = "z", False
+        w["desc"] = (f"complex Hermitian tight-binding {args.size}^3, Peierls phi=1/17, on-site U[-2,2], seed 1, "
+                     f"n={args.size ** 3}, {args.neig} lowest, TOL 1e-10 (matrix uploaded by every solve)")
+    else:
+        K, Mm = M.fem_p1(args.size, sigma=0.5, seed=3)
+        w["A"], w["B"] = K, Mm
+        w["kw"] = dict(isearch=0, sigma=0.0, madspace=20, droptol=1e-3, mem=20.0)
+        w["kind"], w["resident"] = "gep", False
+        w["desc"] = (f"P1-FEM K x = lambda M x, {args.size}x{args.size} nodes, lognormal sigma 0.5, seed 3, "
+                     f"n={(args.size - 2) ** 2}, {args.neig} smallest, TOL 1e-10 (matrices uploaded by every solve)")
+    return w
+
+
+def solve_kwargs(args, icntl2, w=None):
+    kw = dict(w["kw"]) if w is not None else dict(isearch=2, sigma=0.0, madspace=25, droptol=args.droptol,
+                                                   mem=args.mem)
+    kw.update(maxit=100000, tol=1e-10, icntl=(0, icntl2, 0, 0, args.precision))
+    return kw
+
+
 def workload(size):
     from jadamilu_gb300 import matrices as M
-    ia, ja, a = M.anderson3d(size, disorder=16.5, seed=0)
-    return ia, ja, a
+    return M.anderson3d(size, disorder=16.5, seed=0)
 
 
-def solve_kwargs(args, icntl2):
-    return dict(isearch=2, sigma=0.0, madspace=25, maxit=100000, tol=1e-10, droptol=args.droptol, mem=args.mem,
-                icntl=(0, icntl2, 0, 0, args.precision))
+def run_solve(J, w, args, icntl2):
+    a, ja, ia = w["A"][2], w["A"][1], w["A"][0]
+    kw = solve_kwargs(args, icntl2, w)
+    if w["kind"] == "z":
+        return J.zpjd((a, ja, ia), args.neig, **kw)
+    if w["kind"] == "gep":
+        B = w["B"]
+        return J.dpjd_gep((a, ja, ia), (B[2], B[1], B[0]), args.neig, **kw)
+    return J.dpjd((a, ja, ia), args.neig, **kw)
 
 
-def cpu_baseline_sample(J, ia, ja, a, args, gpu_iter):
+def cpu_baseline_sample(J, ia, ja, a, args, gpu_iter, w=None):
     """Oracle iterations on the same matrix with the GPU run's factor."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oracle_lib
@@ -166,14 +236,14 @@ def cpu_baseline_sample(J, ia, ja, a, args, gpu_iter):
     O.orc_dimport_factor.argtypes = [C.c_int] + [C.c_void_p] * 9 + [C.c_double]
     O.orc_dimport_factor(n, p(perm), p(lp), p(li), p(lx), p(blk), p(dinv), p(doff), p(ainv), p(aoff), float(sh[0]))
     # a short capped run gives the cost per MATVEC; a complete solve follows when it fits the budget
-    kw = solve_kwargs(args, -1)
+    kw = solve_kwargs(args, -1, w)
     kw["maxit"] = 16
     t0 = time.perf_counter()
     r = oracle_lib.dpjd(ia, ja, a, args.neig, **kw)
     per_mv = (time.perf_counter() - t0) / max(r["iter"], 1)
     if per_mv * gpu_iter * 1.3 <= args.cpu_seconds:
         t0 = time.perf_counter()
-        r = oracle_lib.dpjd(ia, ja, a, args.neig, **solve_kwargs(args, -1))
+        r = oracle_lib.dpjd(ia, ja, a, args.neig, **solve_kwargs(args, -1, w))
         dt = time.perf_counter() - t0
         return {"value": dt, "unit": "s", "cores": 1, "kind": "port",
                 "sample": f"CPU oracle, same matrix and factor, one complete solve: {r['iter']} MATVECs, "
@@ -201,12 +271,14 @@ def run_gb300(args):
     from jadamilu_gb300 import build
     build.build_all()
     L = J.load()
-    ia, ja, a = workload(args.size)
+    w = make_workload(args)
+    ia, ja, a = w["A"]
     n = len(ia) - 1
     nnz_upper = len(a)
     stream = torch.cuda.Stream()
     J.set_stream(stream.cuda_stream)
-    J.prepare_matrix((a, ja, ia))
+    if w["resident"]:
+        J.prepare_matrix((a, ja, ia))
 
     def barrier():
         if world > 1:
@@ -217,13 +289,13 @@ def run_gb300(args):
     # factorisation (host) + first solve; then warm-up solves reusing the factor
     J.reset_stats()
     t0 = time.perf_counter()
-    r = J.dpjd((a, ja, ia), args.neig, **solve_kwargs(args, 1))
+    r = run_solve(J, w, args, 1)
     first_s = time.perf_counter() - t0
     st = J.stats()
     if r["info"] != 0:
         raise SystemExit(f"first solve failed: INFO={r['info']}")
     for _ in range(max(0, args.warmup - 1)):
-        r = J.dpjd((a, ja, ia), args.neig, **solve_kwargs(args, -1))
+        r = run_solve(J, w, args, -1)
     # timed region: device-resident solves
     clocks = Clocks(local)
     barrier()
@@ -234,7 +306,7 @@ def run_gb300(args):
     iters, results = [], []
     e0.record(stream)
     for _ in range(args.steps):
-        r = J.dpjd((a, ja, ia), args.neig, **solve_kwargs(args, -1))
+        r = run_solve(J, w, args, -1)
         iters.append(r["iter"])
         results.append(r)
     e1.record(stream)
@@ -253,36 +325,45 @@ def run_gb300(args):
     ok = all(rr["info"] == 0 and rr["neig"] == args.neig for rr in results)
     eigs = np.sort(results[-1]["eigs"])
     # roofline of the dominant kernels (preconditioner application) and of SpMV
-    pb = np.zeros(5)
-    L.jdgpu_dprecond_bench.argtypes = [C.c_int, C.c_void_p]
-    L.jdgpu_dprecond_bench(20, pb.ctypes.data_as(C.c_void_p))
-    sb = np.zeros(4)
-    L.jdgpu_dspmv_bench.argtypes = [C.c_int, C.c_void_p]
-    L.jdgpu_dspmv_bench(50, sb.ctypes.data_as(C.c_void_p))
+    # (real standard problems: the resident matrix and the real factor)
+    pb = np.full(5, np.nan)
+    sb = np.full(4, np.nan)
+    if w["resident"]:
+        L.jdgpu_dprecond_bench.argtypes = [C.c_int, C.c_void_p]
+        L.jdgpu_dprecond_bench(20, pb.ctypes.data_as(C.c_void_p))
+        L.jdgpu_dspmv_bench.argtypes = [C.c_int, C.c_void_p]
+        L.jdgpu_dspmv_bench(50, sb.ctypes.data_as(C.c_void_p))
     peak, peak_kind = measured_peaks()
     prec_gbs = pb[1] / (pb[0] * 1e-3) / 1e9
     spmv_gbs = sb[1] / (sb[0] * 1e-3) / 1e9
-    # e2e: through dpjd_ with host buffers (matrix upload + eigenvector download)
-    J.release_matrix()
+    # e2e: through the C ABI with host buffers (matrix upload + eigenvector download)
+    if w["resident"]:
+        J.release_matrix()
     torch.cuda.synchronize()
-    h2d = (n + 1) * 4 + nnz_upper * 4 + nnz_upper * 8
-    d2h = args.neig * n * 8 + 2 * args.neig * 8
+    vb = 16 if w["kind"] == "z" else 8
+    h2d = (n + 1) * 4 + nnz_upper * 4 + nnz_upper * vb
+    if w["B"] is not None:
+        h2d += (n + 1) * 4 + len(w["B"][2]) * 12
+    d2h = args.neig * n * vb + 2 * args.neig * 8
     e2e_s = None
     if not args.no_e2e:
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            J.dpjd((a, ja, ia), args.neig, **solve_kwargs(args, -1))
+            run_solve(J, w, args, -1)
         torch.cuda.synchronize()
         e2e_s = (time.perf_counter() - t0) / args.steps
     cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu:
+    if rank == 0 and world == 1 and not args.no_cpu and w["kind"] == "d":
         try:
-            cpu = cpu_baseline_sample(J, ia, ja, a, args, int(np.median(iters)))
+            cpu = cpu_baseline_sample(J, ia, ja, a, args, int(np.median(iters)), w)
         except Exception as ex:  # reported, not fatal
             cpu = {"value": None, "unit": "s", "cores": 1, "kind": "port", "sample": f"failed: {ex}"}
     if rank == 0:
+        metric = METRIC if w["name"] == "anderson" else f"s to {args.neig} eigpairs at resid 1e-10 ({w['name']})"
+        outer = "c128" if w["kind"] == "z" else "f64"
+        inner = {0: outer, 1: "c64" if w["kind"] == "z" else "f32", 2: "bf16"}[args.precision]
         line = {
-            "metric": METRIC,
+            "metric": metric,
             "value": ms / 1e3,
             "unit": "s",
             "n_gpus": world,
@@ -292,13 +373,11 @@ def run_gb300(args):
             "higher_is_better": False,
             "scaling": "weak",
             "vs_baseline": None,
-            "dtype": "f64 outer / f32 factor" if args.precision == 1 else ("f64" if args.precision == 0 else
-                                                                             "f64 outer / bf16 factor"),
-            "data": "synthetic (seeded splitmix64 Anderson disorder)",
-            "config": {"workload": f"anderson3d {args.size}^3 periodic, W=16.5, seed 0, n={n}, "
-                                   f"{args.neig} eigpairs closest to 0, TOL 1e-10",
-                       "n": n, "nnz_upper": nnz_upper, "droptol": args.droptol, "condest": 5.0,
-                       "madspace": 25, "icntl": [0, -1, 0, 0, args.precision],
+            "dtype": outer if args.precision == 0 else f"{outer} outer / {inner} factor",
+            "data": "synthetic (seeded splitmix64 generators)",
+            "config": {"workload": w["desc"],
+                       "n": n, "nnz_upper": nnz_upper, "droptol": w["kw"]["droptol"], "condest": 5.0,
+                       "madspace": w["kw"]["madspace"], "icntl": [0, -1, 0, 0, args.precision],
                        "factor_s": st["factor_s"], "first_solve_with_factor_s": first_s,
                        "fill": st["fill"], "nnz_l": st["nnz_l"], "levels": st["levels"],
                        "fwd_depth": st["fwd_depth"], "matvec_per_solve": int(np.median(iters)),
@@ -308,7 +387,7 @@ def run_gb300(args):
                        "info": [rr["info"] for rr in results], "neig": [rr["neig"] for rr in results],
                        "max_res": max(float(np.max(rr["res"])) if len(rr["res"]) else 0.0 for rr in results)},
             "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-            "roofline": {"kernel": "ildl_apply graph (level sweeps + dense-tail tile products, fp32)",
+            "roofline": {"kernel": f"ildl_apply graph (level sweeps + dense-block tile products, {inner})",
                          "bound": "hbm",
                          "achieved": prec_gbs, "peak": peak, "unit": "GB/s", "frac": prec_gbs / peak,
                          "traffic": None, "bytes_per_launch": pb[1], "ms_per_launch": pb[0],
@@ -319,7 +398,7 @@ def run_gb300(args):
             "clocks": clk,
             "cpu_baseline": cpu,
         }
-        print(json.dumps(line))
+        print(json.dumps(_finite(line)))
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
@@ -337,25 +416,30 @@ def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
+    w = make_workload(args)
+    if w["kind"] != "d":
+        print(json.dumps({"impl": "reference", "unavailable": "the oracle arm covers the real standard workloads "
+                                                             "(anderson, laplace)"}))
+        return
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oracle_lib
     from jadamilu_gb300 import build
     build.build_oracle()
-    ia, ja, a = workload(args.size)
+    ia, ja, a = w["A"]
     n = len(ia) - 1
     O = oracle_lib.lib()
     threads = os.cpu_count() or 1
     O.orc_set_threads.argtypes = [C.c_int]
     O.orc_set_threads(threads)
     t0 = time.perf_counter()
-    kw = solve_kwargs(args, 1)
+    kw = solve_kwargs(args, 1, w)
     kw["maxit"] = 4
     oracle_lib.dpjd(ia, ja, a, args.neig, **kw)
     factor_s = time.perf_counter() - t0
     mv = int(os.environ.get("JDG_MATVEC_PER_SOLVE", "0")) or None
     times, iters, infos = [], [], []
     for step in range(args.warmup + args.steps):
-        kw = solve_kwargs(args, -1)
+        kw = solve_kwargs(args, -1, w)
         if mv:
             kw["maxit"] = max(16, mv // 10)
         t0 = time.perf_counter()
@@ -369,13 +453,14 @@ def run_reference(args):
     sample = (f"CPU oracle, {'capped samples scaled to %d MATVECs' % mv if mv else 'complete solves'}, "
               f"factor {factor_s:.1f} s on {threads} threads (untimed), solve on 1 core, "
               f"MATVECs {iters}, INFO {infos}")
-    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": world,
+    metric = METRIC if w["name"] == "anderson" else f"s to {args.neig} eigpairs at resid 1e-10 ({w['name']})"
+    line = {"impl": "reference", "metric": metric, "value": v, "unit": "s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64 outer / f32 factor",
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if args.precision == 0 else ("f64 outer / f32 factor" if args.precision == 1
+                                                        else "f64 outer / bf16 factor"),
             "data": "synthetic (seeded splitmix64 Anderson disorder)",
-            "config": {"workload": f"anderson3d {args.size}^3 periodic, W=16.5, seed 0, n={n}, "
-                                   f"{args.neig} eigpairs closest to 0, TOL 1e-10",
-                       "factor_s": factor_s, "matvec_per_solve": int(np.median(iters))},
+            "config": {"workload": w["desc"], "factor_s": factor_s, "matvec_per_solve": int(np.median(iters))},
             "cpu_baseline": {"value": v, "unit": "s", "cores": 1, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))

@@ -71,6 +71,21 @@ JDG_API void djdrevcom_gep_(int* N, double* EIGS, double* RES, double* X, int* L
 /* DPJDCLEANUP: replaces PJDCLEANUP_EV (src/jd/PJD.F:435-488). */
 JDG_API void dpjdcleanup_(void);
 
+/* Legacy drivers PJD, PJDREVCOM, JDREVCOM, PJDCLEANUP (src/jd/PJD_compatible.f:
+ * 3-106): the real drivers above with ICNTL(5) forced to 0; ICNTL(1..4) are
+ * passed through and copied back. */
+JDG_API void pjd_(int* N, double* A, int* JA, int* IA, double* EIGS, double* RES, double* X, int* LX, int* NEIG,
+                  double* SIGMA, int* ISEARCH, int* NINIT, int* MADSPACE, int* ITER, double* TOL, double* SHIFT,
+                  double* DROPTOL, double* MEM, int* ICNTL, int* IPRINT, int* INFO, double* GAP);
+JDG_API void pjdrevcom_(int* N, double* A, int* JA, int* IA, double* EIGS, double* RES, double* X, int* LX, int* NEIG,
+                        double* SIGMA, int* ISEARCH, int* NINIT, int* MADSPACE, int* ITER, double* TOL, double* SHIFT,
+                        double* DROPTOL, double* MEM, int* ICNTL, int* IJOB, int* NDX1, int* NDX2, int* IPRINT,
+                        int* INFO, double* GAP);
+JDG_API void jdrevcom_(int* N, double* EIGS, double* RES, double* X, int* LX, int* NEIG, double* SIGMA, int* ISEARCH,
+                       int* NINIT, int* MADSPACE, int* ITER, double* TOL, int* IJOB, int* NDX1, int* NDX2, int* IPRINT,
+                       int* INFO, double* GAP);
+JDG_API void pjdcleanup_(void);
+
 /* Complex Hermitian versions (ZPJD & co.), same argument meaning with
  * COMPLEX*16 A, B and X (reference C prototypes jadamilu1.h:68-118). */
 JDG_API void zpjd_(int* N, jdg_zcomplex* A, int* JA, int* IA, double* EIGS, double* RES, jdg_zcomplex* X, int* LX,

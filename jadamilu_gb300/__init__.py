@@ -44,8 +44,11 @@ def load(build_if_missing: bool = True):
     _lib = C.CDLL(LIB_PATH)
     L = _lib
     pjd_args = [_P] * 22
-    for name in ("dpjd_", "zpjd_"):
+    for name in ("dpjd_", "zpjd_", "pjd_"):
         getattr(L, name).argtypes = pjd_args
+    L.pjdrevcom_.argtypes = [_P] * 25
+    L.jdrevcom_.argtypes = [_P] * 18
+    L.pjdcleanup_.argtypes = []
     for name in ("dpjd_gep_", "zpjd_gep_"):
         getattr(L, name).argtypes = [_P] * 25
     for name in ("dpjdrevcom_", "zpjdrevcom_"):
@@ -140,7 +143,7 @@ def _matrix(A, dtype):
 
 
 def _pjd(complex_, A, neig, sigma=0.0, isearch=0, ninit=0, madspace=20, maxit=1000, tol=1e-10, shift=0.0,
-         droptol=1e-3, mem=20.0, icntl=(0, 0, 0, 0, 0), iprint=0, x=None, eigs=None, B=None):
+         droptol=1e-3, mem=20.0, icntl=(0, 0, 0, 0, 0), iprint=0, x=None, eigs=None, B=None, legacy=False):
     L = load()
     _require_gpu(L)
     dt = np.complex128 if complex_ else np.float64
@@ -151,13 +154,14 @@ def _pjd(complex_, A, neig, sigma=0.0, isearch=0, ninit=0, madspace=20, maxit=10
     common = [_p(s.EIGS), _p(s.RES), _p(s.X), _p(s.lx), _p(s.NEIG), _p(s.SIGMA), _p(s.ISEARCH), _p(s.NINIT),
               _p(s.MADSPACE), _p(s.ITER), _p(s.TOL), _p(s.SHIFT), _p(s.DROPTOL), _p(s.MEM), _p(s.ICNTL)]
     if B is None:
-        getattr(L, pre + "pjd_")(_p(s.n), _p(a), _p(ja), _p(ia), *common, _p(s.IPRINT), _p(s.INFO), _p(s.GAP))
+        name = "pjd_" if legacy else pre + "pjd_"
+        getattr(L, name)(_p(s.n), _p(a), _p(ja), _p(ia), *common, _p(s.IPRINT), _p(s.INFO), _p(s.GAP))
     else:
         b, jb, ib = _matrix(B, dt)
         getattr(L, pre + "pjd_gep_")(_p(s.n), _p(a), _p(ja), _p(ia), _p(b), _p(jb), _p(ib), *common, _p(s.IPRINT),
                                      _p(s.INFO), _p(s.GAP))
     out = s.result(n)
-    out.update(a=a, ja=ja, ia=ia)
+    out.update(a=a, ja=ja, ia=ia, icntl=s.ICNTL.copy())
     return out
 
 

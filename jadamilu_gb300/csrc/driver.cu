@@ -1390,6 +1390,43 @@ JDG_API void djdrevcom_gep_(int* N, double* EIGS, double* RES, double* X, int* L
 }
 JDG_API void dpjdcleanup_(void) { cleanup_entry<double>(); }
 
+// Legacy entry points (PJD, PJDREVCOM, JDREVCOM, PJDCLEANUP): the real drivers
+// with ICNTL(5) forced to 0 (float64 preconditioner), ICNTL(1..4) passed
+// through and copied back.  The forced copy is static because a
+// reverse-communication solve keeps using it between calls.
+static int g_legacy_icntl[5];
+static void legacy_in(const int* ICNTL) {
+  for (int i = 0; i < 4; ++i) g_legacy_icntl[i] = ICNTL[i];
+  g_legacy_icntl[4] = 0;
+}
+static void legacy_out(int* ICNTL) {
+  for (int i = 0; i < 4; ++i) ICNTL[i] = g_legacy_icntl[i];
+}
+JDG_API void pjd_(int* N, double* A, int* JA, int* IA, double* EIGS, double* RES, double* X, int* LX, int* NEIG,
+                  double* SIGMA, int* ISEARCH, int* NINIT, int* MADSPACE, int* ITER, double* TOL, double* SHIFT,
+                  double* DROPTOL, double* MEM, int* ICNTL, int* IPRINT, int* INFO, double* GAP) {
+  legacy_in(ICNTL);
+  dpjd_(N, A, JA, IA, EIGS, RES, X, LX, NEIG, SIGMA, ISEARCH, NINIT, MADSPACE, ITER, TOL, SHIFT, DROPTOL, MEM,
+        g_legacy_icntl, IPRINT, INFO, GAP);
+  legacy_out(ICNTL);
+}
+JDG_API void pjdrevcom_(int* N, double* A, int* JA, int* IA, double* EIGS, double* RES, double* X, int* LX, int* NEIG,
+                        double* SIGMA, int* ISEARCH, int* NINIT, int* MADSPACE, int* ITER, double* TOL, double* SHIFT,
+                        double* DROPTOL, double* MEM, int* ICNTL, int* IJOB, int* NDX1, int* NDX2, int* IPRINT,
+                        int* INFO, double* GAP) {
+  legacy_in(ICNTL);
+  dpjdrevcom_(N, A, JA, IA, EIGS, RES, X, LX, NEIG, SIGMA, ISEARCH, NINIT, MADSPACE, ITER, TOL, SHIFT, DROPTOL, MEM,
+              g_legacy_icntl, IJOB, NDX1, NDX2, IPRINT, INFO, GAP);
+  legacy_out(ICNTL);
+}
+JDG_API void jdrevcom_(int* N, double* EIGS, double* RES, double* X, int* LX, int* NEIG, double* SIGMA, int* ISEARCH,
+                       int* NINIT, int* MADSPACE, int* ITER, double* TOL, int* IJOB, int* NDX1, int* NDX2, int* IPRINT,
+                       int* INFO, double* GAP) {
+  djdrevcom_(N, EIGS, RES, X, LX, NEIG, SIGMA, ISEARCH, NINIT, MADSPACE, ITER, TOL, IJOB, NDX1, NDX2, IPRINT, INFO,
+             GAP);
+}
+JDG_API void pjdcleanup_(void) { dpjdcleanup_(); }
+
 JDG_API void zpjd_(int* N, zh* A, int* JA, int* IA, double* EIGS, double* RES, zh* X, int* LX, int* NEIG,
                    double* SIGMA, int* ISEARCH, int* NINIT, int* MADSPACE, int* ITER, double* TOL, double* SHIFT,
                    double* DROPTOL, double* MEM, int* ICNTL, int* IPRINT, int* INFO, double* GAP) {

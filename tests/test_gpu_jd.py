@@ -137,3 +137,18 @@ def test_maxit_returns_partial(gpu):
     ia, ja, a = M.laplace3d(8)
     r = gpu.dpjd((a, ja, ia), 10, isearch=0, madspace=10, maxit=25, tol=1e-12, droptol=1e-1)
     assert r["info"] > 0
+
+
+def test_legacy_pjd_forces_float64_preconditioner(gpu, kats):
+    """PJD (src/jd/PJD_compatible.f:3-38) runs DPJD with ICNTL(5) = 0 and
+    leaves the caller's ICNTL(5) as it was."""
+    meta = kats["EXAMPLE1"]
+    A, As, mv, kw = kat_problem(meta)
+    kw = dict(kw, icntl=(0, 0, 0, 0, 1))
+    r_leg = gpu.dpjd((A[2].copy(), A[1].copy(), A[0].copy()), 5, legacy=True, **kw)
+    r_f64 = gpu.dpjd((A[2].copy(), A[1].copy(), A[0].copy()), 5, **dict(kw, icntl=(0, 0, 0, 0, 0)))
+    assert r_leg["info"] == 0 and r_leg["neig"] == 5
+    assert r_leg["icntl"][4] == 1
+    np.testing.assert_array_equal(r_leg["eigs"], r_f64["eigs"])
+    assert r_leg["iter"] == r_f64["iter"]
+    np.testing.assert_allclose(r_leg["eigs"], meta["eigenvalues"], rtol=0, atol=1e-12)
