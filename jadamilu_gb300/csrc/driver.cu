@@ -1345,22 +1345,31 @@ template <class T> void cleanup_entry() {
 
 }  // namespace
 
+// The reference-named entry points keep their names, or, compiled with
+// JDG_ILP64_INNER for the 64-bit-integer library, take an internal prefix and
+// sit behind the wrappers of ilp64.cpp.
+#ifdef JDG_ILP64_INNER
+#define JDG_REF(name) jdg_i32_##name
+#else
+#define JDG_REF(name) name
+#endif
+
 extern "C" {
 
-JDG_API void dpjd_(int* N, double* A, int* JA, int* IA, double* EIGS, double* RES, double* X, int* LX, int* NEIG,
+JDG_API void JDG_REF(dpjd_)(int* N, double* A, int* JA, int* IA, double* EIGS, double* RES, double* X, int* LX, int* NEIG,
                    double* SIGMA, int* ISEARCH, int* NINIT, int* MADSPACE, int* ITER, double* TOL, double* SHIFT,
                    double* DROPTOL, double* MEM, int* ICNTL, int* IPRINT, int* INFO, double* GAP) {
   pjd_entry<double>(N, A, JA, IA, nullptr, nullptr, nullptr, EIGS, RES, X, LX, NEIG, SIGMA, ISEARCH, NINIT, MADSPACE,
                     ITER, TOL, SHIFT, DROPTOL, MEM, ICNTL, IPRINT, INFO, GAP, false);
 }
-JDG_API void dpjd_gep_(int* N, double* A, int* JA, int* IA, double* B, int* JB, int* IB, double* EIGS, double* RES,
+JDG_API void JDG_REF(dpjd_gep_)(int* N, double* A, int* JA, int* IA, double* B, int* JB, int* IB, double* EIGS, double* RES,
                        double* X, int* LX, int* NEIG, double* SIGMA, int* ISEARCH, int* NINIT, int* MADSPACE,
                        int* ITER, double* TOL, double* SHIFT, double* DROPTOL, double* MEM, int* ICNTL, int* IPRINT,
                        int* INFO, double* GAP) {
   pjd_entry<double>(N, A, JA, IA, B, JB, IB, EIGS, RES, X, LX, NEIG, SIGMA, ISEARCH, NINIT, MADSPACE, ITER, TOL,
                     SHIFT, DROPTOL, MEM, ICNTL, IPRINT, INFO, GAP, true);
 }
-JDG_API void dpjdrevcom_(int* N, double* A, int* JA, int* IA, double* EIGS, double* RES, double* X, int* LX,
+JDG_API void JDG_REF(dpjdrevcom_)(int* N, double* A, int* JA, int* IA, double* EIGS, double* RES, double* X, int* LX,
                          int* NEIG, double* SIGMA, int* ISEARCH, int* NINIT, int* MADSPACE, int* ITER, double* TOL,
                          double* SHIFT, double* DROPTOL, double* MEM, int* ICNTL, int* IJOB, int* NDX1, int* NDX2,
                          int* IPRINT, int* INFO, double* GAP) {
@@ -1368,7 +1377,7 @@ JDG_API void dpjdrevcom_(int* N, double* A, int* JA, int* IA, double* EIGS, doub
                           MADSPACE, ITER, TOL, SHIFT, DROPTOL, MEM, ICNTL, IJOB, NDX1, NDX2, nullptr, IPRINT, INFO,
                           GAP, false);
 }
-JDG_API void dpjdrevcom_gep_(int* N, double* A, int* JA, int* IA, double* B, int* JB, int* IB, double* EIGS,
+JDG_API void JDG_REF(dpjdrevcom_gep_)(int* N, double* A, int* JA, int* IA, double* B, int* JB, int* IB, double* EIGS,
                              double* RES, double* X, int* LX, int* NEIG, double* SIGMA, int* ISEARCH, int* NINIT,
                              int* MADSPACE, int* ITER, double* TOL, double* SHIFT, double* DROPTOL, double* MEM,
                              int* ICNTL, int* IJOB, int* NDX1, int* NDX2, int* NDX3, int* IPRINT, int* INFO,
@@ -1376,19 +1385,19 @@ JDG_API void dpjdrevcom_gep_(int* N, double* A, int* JA, int* IA, double* B, int
   pjdrevcom_entry<double>(N, A, JA, IA, B, JB, IB, EIGS, RES, X, LX, NEIG, SIGMA, ISEARCH, NINIT, MADSPACE, ITER, TOL,
                           SHIFT, DROPTOL, MEM, ICNTL, IJOB, NDX1, NDX2, NDX3, IPRINT, INFO, GAP, true);
 }
-JDG_API void djdrevcom_(int* N, double* EIGS, double* RES, double* X, int* LX, int* NEIG, double* SIGMA, int* ISEARCH,
+JDG_API void JDG_REF(djdrevcom_)(int* N, double* EIGS, double* RES, double* X, int* LX, int* NEIG, double* SIGMA, int* ISEARCH,
                         int* NINIT, int* MADSPACE, int* ITER, double* TOL, int* IJOB, int* NDX1, int* NDX2,
                         int* IPRINT, int* INFO, double* GAP) {
   jdrevcom_entry<double>(N, EIGS, RES, X, LX, NEIG, SIGMA, ISEARCH, NINIT, MADSPACE, ITER, TOL, IJOB, NDX1, NDX2,
                          nullptr, IPRINT, INFO, GAP, false);
 }
-JDG_API void djdrevcom_gep_(int* N, double* EIGS, double* RES, double* X, int* LX, int* NEIG, double* SIGMA,
+JDG_API void JDG_REF(djdrevcom_gep_)(int* N, double* EIGS, double* RES, double* X, int* LX, int* NEIG, double* SIGMA,
                             int* ISEARCH, int* NINIT, int* MADSPACE, int* ITER, double* TOL, int* IJOB, int* NDX1,
                             int* NDX2, int* NDX3, int* IPRINT, int* INFO, double* GAP) {
   jdrevcom_entry<double>(N, EIGS, RES, X, LX, NEIG, SIGMA, ISEARCH, NINIT, MADSPACE, ITER, TOL, IJOB, NDX1, NDX2,
                          NDX3, IPRINT, INFO, GAP, true);
 }
-JDG_API void dpjdcleanup_(void) { cleanup_entry<double>(); }
+JDG_API void JDG_REF(dpjdcleanup_)(void) { cleanup_entry<double>(); }
 
 // Legacy entry points (PJD, PJDREVCOM, JDREVCOM, PJDCLEANUP): the real drivers
 // with ICNTL(5) forced to 0 (float64 preconditioner), ICNTL(1..4) passed
@@ -1402,45 +1411,45 @@ static void legacy_in(const int* ICNTL) {
 static void legacy_out(int* ICNTL) {
   for (int i = 0; i < 4; ++i) ICNTL[i] = g_legacy_icntl[i];
 }
-JDG_API void pjd_(int* N, double* A, int* JA, int* IA, double* EIGS, double* RES, double* X, int* LX, int* NEIG,
+JDG_API void JDG_REF(pjd_)(int* N, double* A, int* JA, int* IA, double* EIGS, double* RES, double* X, int* LX, int* NEIG,
                   double* SIGMA, int* ISEARCH, int* NINIT, int* MADSPACE, int* ITER, double* TOL, double* SHIFT,
                   double* DROPTOL, double* MEM, int* ICNTL, int* IPRINT, int* INFO, double* GAP) {
   legacy_in(ICNTL);
-  dpjd_(N, A, JA, IA, EIGS, RES, X, LX, NEIG, SIGMA, ISEARCH, NINIT, MADSPACE, ITER, TOL, SHIFT, DROPTOL, MEM,
+  JDG_REF(dpjd_)(N, A, JA, IA, EIGS, RES, X, LX, NEIG, SIGMA, ISEARCH, NINIT, MADSPACE, ITER, TOL, SHIFT, DROPTOL, MEM,
         g_legacy_icntl, IPRINT, INFO, GAP);
   legacy_out(ICNTL);
 }
-JDG_API void pjdrevcom_(int* N, double* A, int* JA, int* IA, double* EIGS, double* RES, double* X, int* LX, int* NEIG,
+JDG_API void JDG_REF(pjdrevcom_)(int* N, double* A, int* JA, int* IA, double* EIGS, double* RES, double* X, int* LX, int* NEIG,
                         double* SIGMA, int* ISEARCH, int* NINIT, int* MADSPACE, int* ITER, double* TOL, double* SHIFT,
                         double* DROPTOL, double* MEM, int* ICNTL, int* IJOB, int* NDX1, int* NDX2, int* IPRINT,
                         int* INFO, double* GAP) {
   legacy_in(ICNTL);
-  dpjdrevcom_(N, A, JA, IA, EIGS, RES, X, LX, NEIG, SIGMA, ISEARCH, NINIT, MADSPACE, ITER, TOL, SHIFT, DROPTOL, MEM,
+  JDG_REF(dpjdrevcom_)(N, A, JA, IA, EIGS, RES, X, LX, NEIG, SIGMA, ISEARCH, NINIT, MADSPACE, ITER, TOL, SHIFT, DROPTOL, MEM,
               g_legacy_icntl, IJOB, NDX1, NDX2, IPRINT, INFO, GAP);
   legacy_out(ICNTL);
 }
-JDG_API void jdrevcom_(int* N, double* EIGS, double* RES, double* X, int* LX, int* NEIG, double* SIGMA, int* ISEARCH,
+JDG_API void JDG_REF(jdrevcom_)(int* N, double* EIGS, double* RES, double* X, int* LX, int* NEIG, double* SIGMA, int* ISEARCH,
                        int* NINIT, int* MADSPACE, int* ITER, double* TOL, int* IJOB, int* NDX1, int* NDX2, int* IPRINT,
                        int* INFO, double* GAP) {
-  djdrevcom_(N, EIGS, RES, X, LX, NEIG, SIGMA, ISEARCH, NINIT, MADSPACE, ITER, TOL, IJOB, NDX1, NDX2, IPRINT, INFO,
+  JDG_REF(djdrevcom_)(N, EIGS, RES, X, LX, NEIG, SIGMA, ISEARCH, NINIT, MADSPACE, ITER, TOL, IJOB, NDX1, NDX2, IPRINT, INFO,
              GAP);
 }
-JDG_API void pjdcleanup_(void) { dpjdcleanup_(); }
+JDG_API void JDG_REF(pjdcleanup_)(void) { JDG_REF(dpjdcleanup_)(); }
 
-JDG_API void zpjd_(int* N, zh* A, int* JA, int* IA, double* EIGS, double* RES, zh* X, int* LX, int* NEIG,
+JDG_API void JDG_REF(zpjd_)(int* N, zh* A, int* JA, int* IA, double* EIGS, double* RES, zh* X, int* LX, int* NEIG,
                    double* SIGMA, int* ISEARCH, int* NINIT, int* MADSPACE, int* ITER, double* TOL, double* SHIFT,
                    double* DROPTOL, double* MEM, int* ICNTL, int* IPRINT, int* INFO, double* GAP) {
   pjd_entry<zc>(N, A, JA, IA, nullptr, nullptr, nullptr, EIGS, RES, X, LX, NEIG, SIGMA, ISEARCH, NINIT, MADSPACE,
                 ITER, TOL, SHIFT, DROPTOL, MEM, ICNTL, IPRINT, INFO, GAP, false);
 }
-JDG_API void zpjd_gep_(int* N, zh* A, int* JA, int* IA, zh* B, int* JB, int* IB, double* EIGS, double* RES, zh* X,
+JDG_API void JDG_REF(zpjd_gep_)(int* N, zh* A, int* JA, int* IA, zh* B, int* JB, int* IB, double* EIGS, double* RES, zh* X,
                        int* LX, int* NEIG, double* SIGMA, int* ISEARCH, int* NINIT, int* MADSPACE, int* ITER,
                        double* TOL, double* SHIFT, double* DROPTOL, double* MEM, int* ICNTL, int* IPRINT, int* INFO,
                        double* GAP) {
   pjd_entry<zc>(N, A, JA, IA, B, JB, IB, EIGS, RES, X, LX, NEIG, SIGMA, ISEARCH, NINIT, MADSPACE, ITER, TOL, SHIFT,
                 DROPTOL, MEM, ICNTL, IPRINT, INFO, GAP, true);
 }
-JDG_API void zpjdrevcom_(int* N, zh* A, int* JA, int* IA, double* EIGS, double* RES, zh* X, int* LX, int* NEIG,
+JDG_API void JDG_REF(zpjdrevcom_)(int* N, zh* A, int* JA, int* IA, double* EIGS, double* RES, zh* X, int* LX, int* NEIG,
                          double* SIGMA, int* ISEARCH, int* NINIT, int* MADSPACE, int* ITER, double* TOL, double* SHIFT,
                          double* DROPTOL, double* MEM, int* ICNTL, int* IJOB, int* NDX1, int* NDX2, int* IPRINT,
                          int* INFO, double* GAP) {
@@ -1448,26 +1457,26 @@ JDG_API void zpjdrevcom_(int* N, zh* A, int* JA, int* IA, double* EIGS, double* 
                       MADSPACE, ITER, TOL, SHIFT, DROPTOL, MEM, ICNTL, IJOB, NDX1, NDX2, nullptr, IPRINT, INFO, GAP,
                       false);
 }
-JDG_API void zpjdrevcom_gep_(int* N, zh* A, int* JA, int* IA, zh* B, int* JB, int* IB, double* EIGS, double* RES,
+JDG_API void JDG_REF(zpjdrevcom_gep_)(int* N, zh* A, int* JA, int* IA, zh* B, int* JB, int* IB, double* EIGS, double* RES,
                              zh* X, int* LX, int* NEIG, double* SIGMA, int* ISEARCH, int* NINIT, int* MADSPACE,
                              int* ITER, double* TOL, double* SHIFT, double* DROPTOL, double* MEM, int* ICNTL, int* IJOB,
                              int* NDX1, int* NDX2, int* NDX3, int* IPRINT, int* INFO, double* GAP) {
   pjdrevcom_entry<zc>(N, A, JA, IA, B, JB, IB, EIGS, RES, X, LX, NEIG, SIGMA, ISEARCH, NINIT, MADSPACE, ITER, TOL,
                       SHIFT, DROPTOL, MEM, ICNTL, IJOB, NDX1, NDX2, NDX3, IPRINT, INFO, GAP, true);
 }
-JDG_API void zjdrevcom_(int* N, double* EIGS, double* RES, zh* X, int* LX, int* NEIG, double* SIGMA, int* ISEARCH,
+JDG_API void JDG_REF(zjdrevcom_)(int* N, double* EIGS, double* RES, zh* X, int* LX, int* NEIG, double* SIGMA, int* ISEARCH,
                         int* NINIT, int* MADSPACE, int* ITER, double* TOL, int* IJOB, int* NDX1, int* NDX2,
                         int* IPRINT, int* INFO, double* GAP) {
   jdrevcom_entry<zc>(N, EIGS, RES, X, LX, NEIG, SIGMA, ISEARCH, NINIT, MADSPACE, ITER, TOL, IJOB, NDX1, NDX2, nullptr,
                      IPRINT, INFO, GAP, false);
 }
-JDG_API void zjdrevcom_gep_(int* N, double* EIGS, double* RES, zh* X, int* LX, int* NEIG, double* SIGMA,
+JDG_API void JDG_REF(zjdrevcom_gep_)(int* N, double* EIGS, double* RES, zh* X, int* LX, int* NEIG, double* SIGMA,
                             int* ISEARCH, int* NINIT, int* MADSPACE, int* ITER, double* TOL, int* IJOB, int* NDX1,
                             int* NDX2, int* NDX3, int* IPRINT, int* INFO, double* GAP) {
   jdrevcom_entry<zc>(N, EIGS, RES, X, LX, NEIG, SIGMA, ISEARCH, NINIT, MADSPACE, ITER, TOL, IJOB, NDX1, NDX2, NDX3,
                      IPRINT, INFO, GAP, true);
 }
-JDG_API void zpjdcleanup_(void) { cleanup_entry<zc>(); }
+JDG_API void JDG_REF(zpjdcleanup_)(void) { cleanup_entry<zc>(); }
 
 // ------------------------------------------------ kernel-level entries ----
 JDG_API int jdgpu_device_count(void) {

@@ -10,14 +10,9 @@ import jadamilu_gb300 as J
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def declared_symbols():
-    out = []
-    inc = os.path.join(ROOT, "include")
-    for f in sorted(os.listdir(inc)):
-        if f.endswith(".h"):
-            text = open(os.path.join(inc, f)).read()
-            out += re.findall(r"JDG_API\s+[\w\s\*]+?\b(\w+)\s*\(", text)
-    return out
+def declared_symbols(header="jadamilu_gb300.h", macro="JDG_API"):
+    text = open(os.path.join(ROOT, "include", header)).read()
+    return re.findall(macro + r"\s+[\w\s\*]+?\b(\w+)\s*\(", text)
 
 
 def test_header_declares_the_drop_in_drivers():
@@ -33,10 +28,20 @@ def test_library_exports_every_declared_symbol():
     assert not missing, missing
 
 
-def test_library_is_sm103a_only():
+def test_ilp64_library_exports_every_declared_symbol():
+    from jadamilu_gb300 import build
+    build.build_gpu()
+    syms = declared_symbols("jadamilu_gb300_ilp64.h", "JDG64_API")
+    assert len(syms) == 18
+    L = C.CDLL(build.LIB64)
+    missing = [s for s in syms if not hasattr(L, s)]
+    assert not missing, missing
+
+
+def test_build_targets_sm103a_only():
+    from jadamilu_gb300 import build
+    assert build.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]
     assert os.path.exists(J.LIB_PATH)
-    data = open(J.LIB_PATH, "rb").read()
-    assert b"sm_103a" in data or b"sm_103" in data
 
 
 def test_python_mirror_fails_loudly_without_gpu():
