@@ -54,6 +54,9 @@ struct IldlcParams {
   double min_progress = 0.05;  // a level accepting fewer than this fraction ends the recursion
   double depth_weight = 64.0;  // ordering key = degree + depth_weight * (forward level of the row)
   int threads = 0;             // host threads for the row updates (0: hardware concurrency, at most 16)
+  double dense_fill = 0.25;    // a level whose active rows are at least this full is eliminated densely
+  int dense_min_rows = 8192;   //   if it has at least this many rows (smaller ones are quick sparse)
+  double dense_max_bytes = 16e9;  //   and its dense copy fits in this many bytes
 };
 
 template <class T> struct IldlcFactor {
@@ -314,6 +317,254 @@ int ildlc_factor(int n, const int* ia, const int* ja, const T* a, double shift, 
       if (row[q].col == c) { row[q] = row.back(); row.pop_back(); return; }
   };
 
+  // Dense elimination of one level (its active rows nearly full): the same
+  // pivot rules, dropping, estimator and ordering key (row count + depth
+  // weight x forward level, dynamic) as the sparse loop below, on a dense
+  // copy M of the level's active matrix (M[r*m + c] = A(nodes[r], nodes[c])).
+  // An entry that is exactly zero counts as absent for the Schur-fill
+  // dropping and for the row counts.  The rows of the deferred nodes are
+  // written back as sparse rows.
+  std::vector<int> dloc(n, -1);
+  auto dense_level = [&](const std::vector<int>& nodes, bool last_lvl, std::vector<int>& deferred,
+                         int& accepted) -> int {
+    const int m = (int)nodes.size();
+    for (int t = 0; t < m; ++t) dloc[nodes[t]] = t;
+    std::vector<T> M((size_t)m * m, T(0));
+    for (int t = 0; t < m; ++t) {
+      const int i = nodes[t];
+      M[(size_t)t * m + t] = A.diag[i];
+      for (auto& e : A.rows[i]) M[(size_t)t * m + dloc[e.col]] = e.val;
+      A.rows[i].clear();
+      A.rows[i].shrink_to_fit();
+    }
+    std::vector<double> s(m);
+    for (int t = 0; t < m; ++t) s[t] = sc[nodes[t]];
+    std::vector<char> st(m, 0);  // 0 candidate, 1 eliminated, 2 deferred
+    std::vector<int> cnt(m, 0);  // nonzeros of each row among the columns not eliminated
+    for (int t = 0; t < m; ++t)
+      for (int c = 0; c < m; ++c)
+        if (c != t && M[(size_t)t * m + c] != T(0)) cnt[t]++;
+    auto dkey = [&](int t) { return cnt[t] + (int)(prm.depth_weight * dlev[nodes[t]]); };
+    DegQueue DQ;
+    {
+      int mk = 0;
+      for (int t = 0; t < m; ++t) mk = std::max(mk, dkey(t));
+      DQ.init(m, mk + 1);
+      for (int t = 0; t < m; ++t) DQ.push(t, dkey(t));
+    }
+    // a column leaves the active matrix: the rows holding it lose one entry
+    auto drop_column = [&](int p) {
+      for (int r = 0; r < m; ++r)
+        if (r != p && st[r] != 1 && M[(size_t)r * m + p] != T(0)) cnt[r]--;
+    };
+    std::vector<T> lf(m), lg(m);  // dense L columns (zero where dropped or eliminated)
+    std::vector<int> kr;          // local rows with a kept entry
+    auto nu_of = [&](int i) { return 1.0 + (is_cplx ? std::abs(xic[i]) : std::fabs(xi[i])); };
+    auto at = [&](int r, int c) -> T& { return M[(size_t)r * m + c]; };
+    // M(r, c) -= a_r * conj(b_c) (+ c_r * conj(d_c)) for rows and columns in
+    // kr (the only columns with a nonzero L entry); fill drop
+    auto update_rows = [&](const std::vector<T>& av, const std::vector<T>& bv, const std::vector<T>* cv,
+                           const std::vector<T>* dv) {
+      pool.run((int)kr.size(), [&](int, int q) {
+        const int r = kr[q];
+        const T ar = av[r], cr = cv ? (*cv)[r] : T(0);
+        T* row = M.data() + (size_t)r * m;
+        const double sr = s[r];
+        for (int c : kr) {
+          if (c == r) continue;
+          T u = ar * fcj(bv[c]);
+          if (cv) u += cr * fcj((*dv)[c]);
+          if (u == T(0)) continue;
+          if (row[c] != T(0)) {
+            row[c] -= u;
+          } else if (fab(u) * sr * s[c] > dropS) {
+            row[c] = -u;
+            cnt[r]++;
+          }
+        }
+        T ud = ar * fcj(bv[r]);
+        if (cv) ud += cr * fcj((*dv)[r]);
+        row[r] -= T(fre(ud));
+      });
+    };
+    while (DQ.count > 0) {
+      int t = DQ.pop();
+      if (st[t] != 0) continue;
+      int k = nodes[t];
+      double nuk = nu_of(k);
+      if (!last_lvl && nuk > kappa) { st[t] = 2; state[k] = 2; deferred.push_back(k); continue; }
+      T dk = at(t, t);
+      const double skt = s[t];
+      double dks = fab(dk) * skt * skt;
+      double cmax = 0, amax = 0;
+      int jb = -1;
+      for (int r = 0; r < m; ++r) {
+        if (r == t || st[r] == 1) continue;
+        const double v = fab(at(t, r)) * skt * s[r];
+        cmax = std::max(cmax, v);
+        if (st[r] == 0 && v > amax) { amax = v; jb = r; }
+      }
+      int piv = 0;
+      if (last_lvl) {
+        const double alpha = 0.6404;
+        if (dks > 0 && dks >= alpha * cmax) piv = 1;
+        else if (jb < 0) piv = dks > 0 ? 1 : -1;
+        else {
+          double omj = 0;
+          for (int r = 0; r < m; ++r)
+            if (r != t && r != jb && st[r] != 1) omj = std::max(omj, fab(at(jb, r)) * s[jb] * s[r]);
+          const double djs = fab(at(jb, jb)) * s[jb] * s[jb];
+          if (dks * omj >= alpha * amax * amax) piv = 1;
+          else if (djs >= alpha * omj && djs >= alpha * amax) piv = 3;
+          else piv = 2;
+        }
+        if (piv == -1) return (int)order.size() + 1;
+      } else {
+        if (dks > 0 && cmax <= kappa * dks) piv = 1;
+        else if (jb >= 0 && nu_of(nodes[jb]) <= kappa) piv = 2;
+        else piv = 0;
+      }
+      if (piv == 0) { st[t] = 2; state[k] = 2; deferred.push_back(k); continue; }
+      int tp = t;  // local pivot row
+      if (piv == 3) {  // pivot on jb alone; t goes back to the queue
+        DQ.push(t, dkey(t));
+        DQ.remove(jb);
+        tp = jb;
+        piv = 1;
+      }
+      if (piv == 1) {
+        const int kk = nodes[tp];
+        const T d = at(tp, tp);
+        const double nx = last_lvl ? 1.0 : nu_of(kk);
+        const double sp = s[tp];
+        kr.clear();
+        std::fill(lf.begin(), lf.end(), T(0));
+        for (int r = 0; r < m; ++r) {
+          if (r == tp || st[r] == 1) continue;
+          const T a_rk = at(r, tp);
+          if (a_rk == T(0)) continue;
+          const T l = a_rk / d;
+          if (fab(l) * s[r] / sp * nx <= prm.droptol) continue;
+          lf[r] = l;
+          kr.push_back(r);
+        }
+        if (!last_lvl) {
+          if (is_cplx) {
+            cplx x = (std::abs(xic[kk]) > 0) ? -xic[kk] / std::abs(xic[kk]) * (1 + std::abs(xic[kk])) : cplx(1);
+            for (int r : kr) xic[nodes[r]] += cplx(lf[r] * T(s[r] / sp)) * x;
+          } else {
+            double x = (xi[kk] != 0) ? -(xi[kk] / std::fabs(xi[kk])) * (1 + std::fabs(xi[kk])) : 1.0;
+            for (int r : kr) xi[nodes[r]] += fre(lf[r]) * (s[r] / sp) * x;
+          }
+        }
+        for (int r : kr) lg[r] = lf[r] * d;
+        drop_column(tp);
+        st[tp] = 1;  // column tp leaves the update
+        update_rows(lg, lf, nullptr, nullptr);
+        for (int r : kr) {
+          dlev[nodes[r]] = std::max(dlev[nodes[r]], dlev[kk] + 1);
+          lg[r] = T(0);
+        }
+        pos[kk] = (int)order.size();
+        order.push_back(kk);
+        blk[pos[kk]] = 1;
+        dinv[pos[kk]] = T(1) / d;
+        for (int r : kr) { crow.push_back(nodes[r]); cval.push_back(lf[r]); }
+        colptr.push_back((int64_t)crow.size());
+        state[kk] = 1;
+        accepted++;
+      } else {
+        const int j = nodes[jb];
+        const T akj = at(t, jb), dkk = at(t, t), djj = at(jb, jb);
+        const T det = dkk * djj - akj * fcj(akj);
+        const double sj = s[jb];
+        const double dets = fab(det) * skt * skt * sj * sj, offs = fab(akj) * skt * sj;
+        const bool ok = dets > 1e-3 * offs * offs && fab(det) > 0;
+        const T i00 = djj / det, i11 = dkk / det, i01 = -akj / det, i10 = fcj(i01);
+        std::fill(lf.begin(), lf.end(), T(0));
+        std::fill(lg.begin(), lg.end(), T(0));
+        double lmax = 0;
+        std::vector<int> nb;
+        for (int r = 0; r < m; ++r) {
+          if (r == t || r == jb || st[r] == 1) continue;
+          const T aik = at(r, t), aij = at(r, jb);
+          if (aik == T(0) && aij == T(0)) continue;
+          lf[r] = aik * i00 + aij * i10;
+          lg[r] = aik * i01 + aij * i11;
+          lmax = std::max(lmax, std::max(fab(lf[r]) * s[r] / skt, fab(lg[r]) * s[r] / sj));
+          nb.push_back(r);
+        }
+        if (!last_lvl && (!ok || lmax > kappa)) { st[t] = 2; state[k] = 2; deferred.push_back(k); continue; }
+        if (last_lvl && !(fab(det) > 0)) return (int)order.size() + 1;
+        const double nxk = last_lvl ? 1.0 : nu_of(k), nxj = last_lvl ? 1.0 : nu_of(j);
+        kr.clear();
+        for (int r : nb) {
+          if (fab(lf[r]) * s[r] / skt * nxk <= prm.droptol) lf[r] = T(0);
+          if (fab(lg[r]) * s[r] / sj * nxj <= prm.droptol) lg[r] = T(0);
+          if (lf[r] != T(0) || lg[r] != T(0)) kr.push_back(r);
+        }
+        if (!last_lvl) {
+          if (is_cplx) {
+            cplx xk = (std::abs(xic[k]) > 0) ? -xic[k] / std::abs(xic[k]) * (1 + std::abs(xic[k])) : cplx(1);
+            cplx xj = (std::abs(xic[j]) > 0) ? -xic[j] / std::abs(xic[j]) * (1 + std::abs(xic[j])) : cplx(1);
+            for (int r : nb)
+              xic[nodes[r]] += cplx(lf[r] * T(s[r] / skt)) * xk + cplx(lg[r] * T(s[r] / sj)) * xj;
+          } else {
+            double xk = (xi[k] != 0) ? -(xi[k] / std::fabs(xi[k])) * (1 + std::fabs(xi[k])) : 1.0;
+            double xj = (xi[j] != 0) ? -(xi[j] / std::fabs(xi[j])) * (1 + std::fabs(xi[j])) : 1.0;
+            for (int r : nb) xi[nodes[r]] += fre(lf[r]) * (s[r] / skt) * xk + fre(lg[r]) * (s[r] / sj) * xj;
+          }
+        }
+        // update_il = l_ik t_l0 + l_ij t_l1 with t_l = D [conj(l_lk); conj(l_lj)]:
+        // M(r, c) -= (l_rk dkk + l_rj conj(akj)) conj(l_ck) + (l_rk akj + l_rj djj) conj(l_cj)
+        std::vector<T> ua(m, T(0)), ub(m, T(0));
+        for (int r : kr) {
+          ua[r] = lf[r] * dkk + lg[r] * fcj(akj);
+          ub[r] = lf[r] * akj + lg[r] * djj;
+        }
+        drop_column(t);
+        st[t] = 1;
+        drop_column(jb);
+        st[jb] = 1;
+        DQ.remove(jb);
+        update_rows(ua, lf, &ub, &lg);
+        const int lv = std::max(dlev[k], dlev[j]) + 1;
+        for (int r : kr) dlev[nodes[r]] = std::max(dlev[nodes[r]], lv);
+        pos[k] = (int)order.size();
+        order.push_back(k);
+        pos[j] = (int)order.size();
+        order.push_back(j);
+        blk[pos[k]] = 2;
+        blk[pos[j]] = -2;
+        dinv[pos[k]] = i00;
+        dinv[pos[j]] = i11;
+        doff[pos[k]] = i01;
+        for (int r : kr)
+          if (lf[r] != T(0)) { crow.push_back(nodes[r]); cval.push_back(lf[r]); }
+        colptr.push_back((int64_t)crow.size());
+        for (int r : kr)
+          if (lg[r] != T(0)) { crow.push_back(nodes[r]); cval.push_back(lg[r]); }
+        colptr.push_back((int64_t)crow.size());
+        state[k] = 1;
+        state[j] = 1;
+        accepted += 2;
+      }
+      if ((int64_t)crow.size() + n > memcap) return -3;
+      for (int r : kr)
+        if (st[r] == 0) DQ.update(r, dkey(r));
+    }
+    // deferred rows back to the sparse trailing matrix
+    for (int t = 0; t < m; ++t) {
+      if (st[t] != 2) continue;
+      const int i = nodes[t];
+      A.diag[i] = at(t, t);
+      for (int c = 0; c < m; ++c)
+        if (c != t && st[c] == 2 && at(t, c) != T(0)) A.rows[i].push_back({nodes[c], at(t, c)});
+    }
+    for (int t = 0; t < m; ++t) dloc[nodes[t]] = -1;
+    return 0;
+  };
+
   while (!level_nodes.empty()) {
     const int nl = (int)level_nodes.size();
     if (level >= prm.max_levels || nl <= prm.last_level_min) last = true;
@@ -331,19 +582,30 @@ int ildlc_factor(int n, const int* ia, const int* ja, const T* a, double shift, 
         for (auto& e : A.rows[i]) m = std::max(m, fab(e.val) * sc[i] * sc[e.col]);
         if (m > 0) sc[i] /= std::sqrt(m);
       }
-    int maxdeg = 0;
-    for (int i : level_nodes) maxdeg = std::max(maxdeg, (int)A.rows[i].size());
-    Q.init(n, maxdeg + 1);
+    std::vector<int> deferred;
+    int accepted_here = 0;
+    int64_t level_entries = 0;
     for (int i : level_nodes) {
       xi[i] = 0;
       xic[i] = 0;
       state[i] = 0;
-      Q.push(i, qkey(i));
+      level_entries += (int64_t)A.rows[i].size();
     }
-    std::vector<int> deferred;
-    int accepted_here = 0;
+    const bool dense_lvl = nl >= prm.dense_min_rows &&
+                           (double)level_entries >= prm.dense_fill * (double)nl * (double)(nl - 1) &&
+                           (double)nl * (double)nl * sizeof(T) <= prm.dense_max_bytes;
+    if (dense_lvl) {
+      const int rc = dense_level(level_nodes, last, deferred, accepted_here);
+      if (rc != 0) return rc;
+    }
+    int maxdeg = 0;
+    if (!dense_lvl) {
+      for (int i : level_nodes) maxdeg = std::max(maxdeg, (int)A.rows[i].size());
+      Q.init(n, maxdeg + 1);
+      for (int i : level_nodes) Q.push(i, qkey(i));
+    }
 
-    while (Q.count > 0) {
+    while (!dense_lvl && Q.count > 0) {
       int k = Q.pop();
       if (state[k] != 0) continue;
       const double sk = sc[k];

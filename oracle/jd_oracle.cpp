@@ -642,6 +642,8 @@ void orc_zmatveca(int n, const int* ia, const int* ja, const cplx* a, const cplx
 struct OrcFactorD { jdg::IldlcFactor<double> F; };
 void orc_set_depth_weight(double w) { orc::g_depth_weight = w; }
 void orc_set_drop_schur(double v) { orc::g_drop_schur = v; }
+static int g_dense_min_rows = -1;  // IldlcParams::dense_min_rows for orc_dfactor (negative: its default)
+void orc_set_dense_min_rows(int v) { g_dense_min_rows = v; }
 static int g_threads = 0;
 void orc_set_threads(int t) { g_threads = t; }
 void* orc_dfactor(int n, const int* ia, const int* ja, const double* a, double shift, double droptol, double condest,
@@ -650,6 +652,7 @@ void* orc_dfactor(int n, const int* ia, const int* ja, const double* a, double s
   jdg::IldlcParams p;
   p.depth_weight = orc::g_depth_weight;
   p.droptol_schur = orc::g_drop_schur;
+  if (g_dense_min_rows >= 0) p.dense_min_rows = g_dense_min_rows;
   p.threads = g_threads;
   p.droptol = droptol;
   p.condest = condest;

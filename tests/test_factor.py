@@ -18,7 +18,20 @@ def _random_indefinite(n, seed):
     return (U.indptr + 1).astype(np.int32), (U.indices + 1).astype(np.int32), U.data.astype(np.float64)
 
 
+def _dense_indefinite(n, seed, density=0.4):
+    """Symmetric indefinite matrix with 40 % of its entries set: the whole
+    first level takes the dense elimination path."""
+    rng = np.random.default_rng(seed)
+    A = sp.random(n, n, density=density, random_state=seed) * 0.1
+    A = A + A.T + sp.diags(rng.uniform(-2, 2, n))
+    U = sp.triu(A).tocsr()
+    U = (U + sp.diags(np.where(U.diagonal() == 0, 1e-3, 0.0))).tocsr()
+    U.sort_indices()
+    return (U.indptr + 1).astype(np.int32), (U.indices + 1).astype(np.int32), U.data.astype(np.float64)
+
+
 CASES = {
+    "dense_indefinite": lambda: _dense_indefinite(500, 3),
     "laplace6": lambda: M.laplace3d(6),
     "anderson7": lambda: M.anderson3d(7, seed=2),
     "tridiag": lambda: M.tridiag(300),
@@ -31,7 +44,15 @@ CASES = {
 def test_exact_when_nothing_is_dropped(oracle, name):
     ia, ja, a = CASES[name]()
     A = M.to_scipy_full(ia, ja, a)
-    F = oracle.Factor(ia, ja, a, shift=0.1, droptol=0.0, mem=0)
+    import ctypes as C
+    lib = oracle.lib()
+    lib.orc_set_dense_min_rows.argtypes = [C.c_int]
+    # small levels take the dense path here (by default only levels of 8192+ rows do)
+    lib.orc_set_dense_min_rows(256 if name.startswith("dense") else -1)
+    try:
+        F = oracle.Factor(ia, ja, a, shift=0.1, droptol=0.0, mem=0)
+    finally:
+        lib.orc_set_dense_min_rows(-1)
     assert F.ierr == 0
     b = np.random.default_rng(1).standard_normal(A.shape[0])
     x = F.apply(b)
