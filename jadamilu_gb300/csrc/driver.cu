@@ -1876,6 +1876,7 @@ JDG_API void jdgpu_set_option(const char* name, double value) {
   else if (!std::strcmp(name, "dense_tail")) g_opt.dense_tail = (int)value;
   else if (!std::strcmp(name, "dense_max")) g_opt.dense_max = (int)value;
   else if (!std::strcmp(name, "drop_schur")) g_opt.drop_schur = value;
+  else if (!std::strcmp(name, "pdl")) k::set_pdl(value != 0);
   else if (!std::strcmp(name, "apply_graph")) g_opt.apply_graph = (int)value;
   else if (!std::strcmp(name, "verbose")) g_opt.verbose = (int)value;
 }

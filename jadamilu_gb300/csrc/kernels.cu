@@ -19,6 +19,32 @@ void add_launches(long long n) { g_launches += n; }
 #define COUNT_LAUNCH() (g_launches += 1)
 
 constexpr int TPB = 256;
+
+// Programmatic dependent launch inside the preconditioner graph: a kernel
+// lets its successor be scheduled as soon as all of its CTAs have started
+// (launch_dependents), and waits for its predecessor to complete and flush
+// (griddepcontrol.wait) before reading anything.  Both are no-ops for a
+// kernel launched without the attribute.
+__device__ __forceinline__ void pdl_begin() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+static bool g_pdl = true;
+void set_pdl(bool on) { g_pdl = on; }
+template <class... Params, class... Args>
+static void launch_k(void (*kern)(Params...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = g_pdl ? 1 : 0;
+  CK(cudaLaunchKernelEx(&cfg, kern, static_cast<Params>(args)...));
+}
 static inline int nblk(long n, int tpb = TPB) { return (int)std::max<long>(1, (n + tpb - 1) / tpb); }
 
 // ---------------------------------------------------------------- SpMV ----
@@ -229,17 +255,20 @@ template <class T> void diagsolve(long n, const double* d, const T* rhs, T* sol,
 // ------------------------------------------------ multilevel LDL^H apply ----
 template <class T, class A>
 __global__ void ildl_gather_kernel(int n, const int* __restrict__ orig, const T* __restrict__ b, A* __restrict__ y) {
+  pdl_begin();
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s < n) y[s] = cvt<A>(b[orig[s]]);
 }
 template <class T, class A>
 __global__ void ildl_scatter_kernel(int n, const int* __restrict__ orig, const A* __restrict__ y, T* __restrict__ x) {
+  pdl_begin();
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s < n) x[orig[s]] = cvt<T>(y[s]);
 }
 template <class S, class A>
 __global__ void ildl_dsolve_kernel(int n, const signed char* __restrict__ blk, const int* __restrict__ partner,
                                    const S* __restrict__ dv, const S* __restrict__ dof, A* __restrict__ y) {
+  pdl_begin();
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
   signed char b = blk[s];
@@ -274,6 +303,7 @@ __global__ void __launch_bounds__(RUN_TPB) ildl_run_kernel(int l0, int l1, const
                                                           const int* __restrict__ rows, const int64_t* __restrict__ rp,
                                                           const int* __restrict__ ci, const S* __restrict__ cv,
                                                           A* y) {
+  pdl_begin();
   __shared__ A part[RUN_WARPS];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int l = l0; l < l1; ++l) {
@@ -320,6 +350,7 @@ template <class S, class A, int LANES>
 __global__ void __launch_bounds__(WIDE_TPB) ildl_wide_kernel(int lo, int hi, const int* __restrict__ rows,
                                                             const int64_t* __restrict__ rp, const int* __restrict__ ci,
                                                             const S* __restrict__ cv, A* __restrict__ y) {
+  pdl_begin();
   const int g = blockIdx.x * (WIDE_TPB / LANES) + (threadIdx.x / LANES);
   const int lane = threadIdx.x % LANES;
   const int t = lo + g;
@@ -341,6 +372,7 @@ template <class S, class A, int LANES>
 __global__ void __launch_bounds__(WIDE_TPB) tail_ext_kernel(int m, int s_tail, const int64_t* __restrict__ rp,
                                                            const int* __restrict__ ci, const S* __restrict__ cv,
                                                            A* __restrict__ y) {
+  pdl_begin();
   const int t = blockIdx.x * (WIDE_TPB / LANES) + (threadIdx.x / LANES);
   const int lane = threadIdx.x % LANES;
   A acc = A(0);
@@ -353,16 +385,16 @@ template <class S, class A>
 static void launch_wide(int lanes, int lo, int hi, const int* rows, const int64_t* rp, const int* ci, const S* cv, A* y,
                         cudaStream_t s) {
   const int nb = (hi - lo) * lanes / WIDE_TPB + 1;
-  if (lanes == 32) ildl_wide_kernel<S, A, 32><<<nb, WIDE_TPB, 0, s>>>(lo, hi, rows, rp, ci, cv, y);
-  else if (lanes == 16) ildl_wide_kernel<S, A, 16><<<nb, WIDE_TPB, 0, s>>>(lo, hi, rows, rp, ci, cv, y);
-  else ildl_wide_kernel<S, A, 8><<<nb, WIDE_TPB, 0, s>>>(lo, hi, rows, rp, ci, cv, y);
+  if (lanes == 32) launch_k(ildl_wide_kernel<S, A, 32>, dim3(nb), dim3(WIDE_TPB), 0, s, lo, hi, rows, rp, ci, cv, y);
+  else if (lanes == 16) launch_k(ildl_wide_kernel<S, A, 16>, dim3(nb), dim3(WIDE_TPB), 0, s, lo, hi, rows, rp, ci, cv, y);
+  else launch_k(ildl_wide_kernel<S, A, 8>, dim3(nb), dim3(WIDE_TPB), 0, s, lo, hi, rows, rp, ci, cv, y);
 }
 template <class S, class A>
 static void launch_ext(int lanes, int m, int s0, const int64_t* rp, const int* ci, const S* cv, A* y, cudaStream_t s) {
   const int nb = m * lanes / WIDE_TPB + 1;
-  if (lanes == 32) tail_ext_kernel<S, A, 32><<<nb, WIDE_TPB, 0, s>>>(m, s0, rp, ci, cv, y);
-  else if (lanes == 16) tail_ext_kernel<S, A, 16><<<nb, WIDE_TPB, 0, s>>>(m, s0, rp, ci, cv, y);
-  else tail_ext_kernel<S, A, 8><<<nb, WIDE_TPB, 0, s>>>(m, s0, rp, ci, cv, y);
+  if (lanes == 32) launch_k(tail_ext_kernel<S, A, 32>, dim3(nb), dim3(WIDE_TPB), 0, s, m, s0, rp, ci, cv, y);
+  else if (lanes == 16) launch_k(tail_ext_kernel<S, A, 16>, dim3(nb), dim3(WIDE_TPB), 0, s, m, s0, rp, ci, cv, y);
+  else launch_k(tail_ext_kernel<S, A, 8>, dim3(nb), dim3(WIDE_TPB), 0, s, m, s0, rp, ci, cv, y);
 }
 // The sequential part of a tail sweep in one CTA.  Shared memory holds the
 // tail of y (yt), the row pointers relative to the first tail entry, the level
@@ -378,6 +410,7 @@ __global__ void __launch_bounds__(RUN_TPB) tail_run_kernel(int m, int s_tail, in
                                                           const int* __restrict__ rows, const int64_t* __restrict__ rp,
                                                           const int* __restrict__ ci, const S* __restrict__ cv,
                                                           A* __restrict__ y) {
+  pdl_begin();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   A* yt = reinterpret_cast<A*>(smem_raw);
   int* srp = reinterpret_cast<int*>(smem_raw + ((sizeof(A) * (size_t)m + 15) / 16) * 16);
@@ -481,6 +514,7 @@ template <class S, class A>
 __global__ void __launch_bounds__(TRI_TPB) tri_partial_kernel(const int4* __restrict__ items,
                                                              const S* __restrict__ tiles, const A* __restrict__ x,
                                                              int m, A* __restrict__ part) {
+  pdl_begin();
   constexpr int V = 16 / sizeof(S);   // elements per 16-byte vector
   constexpr int RG = 64 / V;          // vectors per tile column
   constexpr int CPS = TRI_TPB / RG;   // tile columns covered by one pass of the CTA
@@ -523,6 +557,7 @@ __global__ void __launch_bounds__(TRI_TPB) tri_partial_kernel(const int4* __rest
 }
 template <class A>
 __global__ void tri_reduce_kernel(int m, const int* __restrict__ irow, const A* __restrict__ part, A* __restrict__ y) {
+  pdl_begin();
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= m) return;
   const int i = e >> 6, r = e & 63;
@@ -600,13 +635,13 @@ template <class S> void ildl_plan_bwd0(DevFactor<S>& F, const std::vector<int64_
 template <class T, class S> void ildl_apply(const DevFactor<S>& F, bool spd, const T* b, T* x, cudaStream_t s) {
   using A = typename Arith<S>::type;
   const int n = F.n;
-  ildl_gather_kernel<T, A><<<nblk(n), TPB, 0, s>>>(n, F.orig, b, F.y);
+  launch_k(ildl_gather_kernel<T, A>, dim3(nblk(n)), dim3(TPB), 0, s, n, F.orig, b, F.y);
   auto sweep = [&](const std::vector<int>& seg, const std::vector<int>& ptr, const int* dptr, const int* rows,
                    const int64_t* rp, const int* ci, const S* cv) {
     for (size_t q = 0; q < seg.size(); q += 3) {
       int l0 = seg[q], l1 = seg[q + 1];
       if (seg[q + 2] == 1) {
-        ildl_run_kernel<S, A><<<1, RUN_TPB, 0, s>>>(l0, l1, dptr, rows, rp, ci, cv, F.y);
+        launch_k(ildl_run_kernel<S, A>, dim3(1), dim3(RUN_TPB), 0, s, l0, l1, dptr, rows, rp, ci, cv, F.y);
       } else {
         launch_wide<S, A>(seg[q + 2], ptr[l0], ptr[l0 + 1], rows, rp, ci, cv, F.y, s);
       }
@@ -626,32 +661,32 @@ template <class T, class S> void ildl_apply(const DevFactor<S>& F, bool spd, con
       A* yb = F.y + B.s0;
       if (B.nfe > 0) ext(B.m, B.s0, B.ep, B.ei, B.ev, B.nfe);
       if (B.nt > 0) {
-        tri_partial_kernel<S, A><<<B.nitf, TRI_TPB, 0, s>>>((const int4*)B.itf, B.tf, yb, B.m, F.part);
-        tri_reduce_kernel<A><<<nblk(B.m), TPB, 0, s>>>(B.m, B.irf, F.part, yb);
+        launch_k(tri_partial_kernel<S, A>, dim3(B.nitf), dim3(TRI_TPB), 0, s, (const int4*)B.itf, B.tf, yb, B.m, F.part);
+        launch_k(tri_reduce_kernel<A>, dim3(nblk(B.m)), dim3(TPB), 0, s, B.m, B.irf, F.part, yb);
       }
     }
   } else if (levels) {
     ext(F.m_tail, F.s_tail, F.tep, F.tei, F.tev, 8 * (int64_t)F.m_tail);
-    tail_run_kernel<S, A><<<1, RUN_TPB, tsm, s>>>(F.m_tail, F.s_tail, (int)F.tfptr.size() - 1, F.dtfptr, nullptr,
+    launch_k(tail_run_kernel<S, A>, dim3(1), dim3(RUN_TPB), tsm, s, F.m_tail, F.s_tail, (int)F.tfptr.size() - 1, F.dtfptr, nullptr,
                                                  F.tip, F.tii, F.tiv, F.y);
   }
-  ildl_dsolve_kernel<S, A><<<nblk(n), TPB, 0, s>>>(n, F.blk, F.partner, spd ? F.av : F.dv, spd ? F.aof : F.dof, F.y);
+  launch_k(ildl_dsolve_kernel<S, A>, dim3(nblk(n)), dim3(TPB), 0, s, n, F.blk, F.partner, spd ? F.av : F.dv, spd ? F.aof : F.dof, F.y);
   if (dense) {
     for (auto it = F.blocks.rbegin(); it != F.blocks.rend(); ++it) {
       const auto& B = *it;
       A* yb = F.y + B.s0;
       if (B.nbe > 0) ext(B.m, B.s0, B.bp, B.bi, B.bv, B.nbe);
       if (B.nt > 0) {
-        tri_partial_kernel<S, A><<<B.nitb, TRI_TPB, 0, s>>>((const int4*)B.itb, B.tb, yb, B.m, F.part);
-        tri_reduce_kernel<A><<<nblk(B.m), TPB, 0, s>>>(B.m, B.irb, F.part, yb);
+        launch_k(tri_partial_kernel<S, A>, dim3(B.nitb), dim3(TRI_TPB), 0, s, (const int4*)B.itb, B.tb, yb, B.m, F.part);
+        launch_k(tri_reduce_kernel<A>, dim3(nblk(B.m)), dim3(TPB), 0, s, B.m, B.irb, F.part, yb);
       }
     }
   } else if (levels) {
-    tail_run_kernel<S, A><<<1, RUN_TPB, tsm, s>>>(F.m_tail, F.s_tail, (int)F.tbptr.size() - 1, F.dtbptr, F.tbrows,
+    launch_k(tail_run_kernel<S, A>, dim3(1), dim3(RUN_TPB), tsm, s, F.m_tail, F.s_tail, (int)F.tbptr.size() - 1, F.dtbptr, F.tbrows,
                                                  F.tbp, F.tbi, F.tbv, F.y);
   }
   sweep(F.bseg, F.bptr, F.dbptr, F.brows, F.up, F.ui, F.ux);
-  ildl_scatter_kernel<T, A><<<nblk(n), TPB, 0, s>>>(n, F.orig, F.y, x);
+  launch_k(ildl_scatter_kernel<T, A>, dim3(nblk(n)), dim3(TPB), 0, s, n, F.orig, F.y, x);
 }
 
 template <class T, class S> void ildl_apply_graph(DevFactor<S>& F, bool spd, const T* b, T* x, cudaStream_t s) {

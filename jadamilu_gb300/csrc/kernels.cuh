@@ -85,6 +85,8 @@ namespace k {
 
 // kernels launched by this library so far (graph replays count their kernel nodes)
 long long launch_count();
+// programmatic dependent launch between the preconditioner's kernels (default on)
+void set_pdl(bool on);
 void add_launches(long long n);
 
 template <class T> void spmv(const SellMatrix<T>& A, const T* x, T* y, cudaStream_t s);
