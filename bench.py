@@ -53,10 +53,13 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="anderson", choices=["anderson", "laplace", "tightbinding", "fem"],
+    ap.add_argument("--batch", type=int, default=64, help="batch workload: number of problems (512 is the named case)")
+    ap.add_argument("--workers", type=int, default=16, help="batch workload: host worker threads / CUDA streams")
+    ap.add_argument("--workload", default="anderson", choices=["anderson", "laplace", "tightbinding", "fem", "batch"],
                     help="anderson: the headline 3-D Anderson model (default); laplace: 20^3 Dirichlet Laplacian, "
                          "plain float64; tightbinding: complex Hermitian 64^3 Peierls model, complex64 factor; "
-                         "fem: P1-FEM K x = lambda M x, 512^2 nodes, float64")
+                         "fem: P1-FEM K x = lambda M x, 512^2 nodes, float64; batch: --batch Anderson problems, "
+                         "edges uniform in 16..40, 5 eigpairs closest to 0 each, float32 factor")
     ap.add_argument("--size", type=int, default=None,
                     help="lattice edge m (anderson: n = m^3, default %d, 100 is the named 1e6 case; laplace 20; "
                          "tightbinding 64; fem: nodes per side, 512)" % DEFAULT_SIZE)
@@ -70,7 +73,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     args = ap.parse_args()
     defaults = {"anderson": (DEFAULT_SIZE, 1, 10), "laplace": (20, 0, 10), "tightbinding": (64, 1, 8),
-                "fem": (512, 0, 6)}[args.workload]
+                "fem": (512, 0, 6), "batch": (40, 1, 5)}[args.workload]
     if args.size is None:
         args.size = defaults[0]
     if args.precision is None:
@@ -416,6 +419,10 @@ def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
+    if args.workload == "batch":
+        print(json.dumps({"impl": "reference", "unavailable": "the oracle arm covers the real standard workloads "
+                                                             "(anderson, laplace)"}))
+        return
     w = make_workload(args)
     if w["kind"] != "d":
         print(json.dumps({"impl": "reference", "unavailable": "the oracle arm covers the real standard workloads "
@@ -466,10 +473,73 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def run_batch(args):
+    """Batched workload: --batch independent Anderson problems (edges uniform
+    in 16..40 from seed 2, W=16.5, disorder seeds 1000+q), 5 eigenpairs closest
+    to 0 each, solved by jdgpu_dpjd_batch with --workers threads / streams.
+    A step is one batch call, host ILDLC factorisations included (every
+    problem gets its own preconditioner); wall clock around the call."""
+    rank, world, local = dist_env()
+    import torch
+    torch.cuda.set_device(local)
+    import jadamilu_gb300 as J
+    from jadamilu_gb300 import build
+    from jadamilu_gb300 import matrices as M
+    build.build_all()
+    L = J.load()
+    edges = np.random.default_rng(2).integers(16, 41, size=args.batch)
+    probs = [M.anderson3d(int(m), disorder=16.5, seed=1000 + q) for q, m in enumerate(edges)]
+    mats = [(a, ja, ia) for ia, ja, a in probs]
+    kw = dict(sigma=0.0, isearch=2, madspace=20, maxit=100000, tol=1e-10, droptol=args.droptol, mem=args.mem,
+              icntl=(0, 0, 0, 0, args.precision))
+
+    def one():
+        fresh = [(a.copy(), ja.copy(), ia.copy()) for a, ja, ia in mats]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = J.dpjd_batch(fresh, args.neig, workers=args.workers, **kw)
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0, out
+
+    for _ in range(args.warmup):
+        one()
+    clocks = Clocks(local)
+    clocks.start()
+    l0 = L.jdgpu_launch_count()
+    times, outs = [], None
+    for _ in range(args.steps):
+        dt, outs = one()
+        times.append(dt)
+    launches = L.jdgpu_launch_count() - l0
+    clk = clocks.stop()
+    v = float(np.mean(times))
+    ok = all(r["info"] == 0 and r["neig"] == args.neig for r in outs)
+    n_tot = int(sum(int(m) ** 3 for m in edges))
+    h2d = int(sum((len(ia) + len(ja)) * 4 + len(a) * 8 for a, ja, ia in mats))
+    d2h = int(sum(int(m) ** 3 * args.neig * 8 for m in edges))
+    line = {"metric": f"s to {args.neig} eigpairs per problem at resid 1e-10, batch of {args.batch} Anderson problems",
+            "value": v, "unit": "s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": v * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64 outer / f32 factor" if args.precision == 1 else "f64",
+            "data": "synthetic (seeded splitmix64 generators)",
+            "config": {"workload": f"{args.batch} Anderson problems, edges 16..40 (seed 2), n total {n_tot}, "
+                                   f"{args.neig} eigpairs closest to 0 each, TOL 1e-10, host ILDLC per problem "
+                                   f"included",
+                       "workers": args.workers, "droptol": args.droptol, "converged": ok,
+                       "matvec_total": int(sum(r["iter"] for r in outs)),
+                       "info_nonzero": int(sum(r["info"] != 0 for r in outs))},
+            "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "roofline": None, "gpu_launches": int(launches), "clocks": clk, "cpu_baseline": None}
+    if rank == 0:
+        print(json.dumps(_finite(line)))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batch":
+        run_batch(args)
     else:
         run_gb300(args)
 

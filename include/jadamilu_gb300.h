@@ -199,6 +199,23 @@ JDG_API int jdgpu_dildl_apply_noalloc(int n, const int* ia, const int* ja, const
 JDG_API int jdgpu_deig_grad(int n, const int* ia, const int* ja, int neig, const double* X, int ldx,
                             const double* w, const double* bdiag, double* grad);
 
+/* Batched DPJD: nprob independent real symmetric problems solved by
+ * nworkers host threads, each with its own solver state and CUDA stream, so
+ * several solves run on the GPU at once; problems are taken largest first.
+ * Per problem q (arrays of pointers / values indexed by q), as in DPJD:
+ * n[q], a[q]/ja[q]/ia[q] (modified as by DPJD), eigs[q], res[q], x[q] (LX =
+ * lx[q] entries), neig[q] (in: wanted, out: converged), iter[q] (in: MATVEC
+ * budget, out: used), info[q], gap[q] (may be NULL).  Shared: sigma,
+ * isearch, madspace, tol, droptol, mem and icntl (ICNTL(2) is taken as 0:
+ * every problem gets its own preconditioner).  No NINIT, no printing.
+ * Extension for the batched configuration; the drop-in drivers keep the
+ * reference's one-solve-per-process state.  Returns 0, or -1 on bad
+ * arguments. */
+JDG_API int jdgpu_dpjd_batch(int nprob, const int* n, double* const* a, int* const* ja, int* const* ia,
+                             double* const* eigs, double* const* res, double* const* x, const int* lx, int* neig,
+                             int* iter, int* info, double* gap, double sigma, int isearch, int madspace, double tol,
+                             double droptol, double mem, const int* icntl, int nworkers);
+
 /* Options: "depth_weight" (ordering key weight of the triangular-solve
  * depth, default 64), "verbose", "dense_tail" (1: solve the deepest levels of
  * the preconditioner with the explicit inverse of their block, default; 0:

@@ -292,6 +292,43 @@ def ildl_apply(A, b, shift=0.0, droptol=1e-3, condest=5.0, spd=False, precision=
     return X.reshape(b.shape), dict(zip(keys, info.tolist()))
 
 
+def dpjd_batch(problems, neig, workers=8, sigma=0.0, isearch=2, madspace=20, maxit=10000, tol=1e-10,
+               droptol=1e-3, mem=20.0, icntl=(0, 0, 0, 0, 1)):
+    """Solve independent real symmetric problems [(a, ja, ia), ...] with
+    jdgpu_dpjd_batch (worker threads with their own solver state and CUDA
+    stream).  Returns one result dict per problem (eigs, res, x, neig, iter,
+    info, gap)."""
+    L = load()
+    _require_gpu(L)
+    P = len(problems)
+    mats = [_matrix(A, np.float64) for A in problems]
+    n = np.array([len(m[2]) - 1 for m in mats], np.int32)
+    lx = np.array([k * (3 * madspace + neig + 4) + 3 * madspace * madspace + max(madspace * madspace, neig)
+                   for k in n], np.int32)
+    X = [np.zeros(int(v)) for v in lx]
+    E = [np.zeros(neig) for _ in range(P)]
+    R = [np.zeros(neig) for _ in range(P)]
+    ptrs = lambda arrs: (C.c_void_p * P)(*[a.ctypes.data for a in arrs])
+    NEIG = np.full(P, neig, np.int32)
+    ITER = np.full(P, maxit, np.int32)
+    INFO = np.zeros(P, np.int32)
+    GAP = np.zeros(P)
+    ic = np.array(icntl, np.int32)
+    L.jdgpu_dpjd_batch.argtypes = [C.c_int, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, C.c_double, C.c_int,
+                                   C.c_int, C.c_double, C.c_double, C.c_double, _P, C.c_int]
+    rc = L.jdgpu_dpjd_batch(P, _p(n), ptrs([m[0] for m in mats]), ptrs([m[1] for m in mats]),
+                            ptrs([m[2] for m in mats]), ptrs(E), ptrs(R), ptrs(X), _p(lx), _p(NEIG), _p(ITER),
+                            _p(INFO), _p(GAP), sigma, isearch, madspace, tol, droptol, mem, _p(ic), workers)
+    if rc != 0:
+        raise RuntimeError(f"jdgpu_dpjd_batch failed ({rc})")
+    out = []
+    for q in range(P):
+        k = int(NEIG[q])
+        out.append(dict(eigs=E[q][:k].copy(), res=R[q][:k].copy(), x=X[q][:n[q] * k].reshape(k, n[q]).T.copy(),
+                        neig=k, iter=int(ITER[q]), info=int(INFO[q]), gap=float(GAP[q])))
+    return out
+
+
 def eig_grad(A, X, w=None, bdiag=None):
     """Gradient of sum_k w[k] * lambda_k with respect to the stored entries of
     A = (a, ja, ia), from eigenvectors X (n x k, columns; any scaling) of

@@ -79,6 +79,19 @@ template <class T> struct Workspace {
     N = n;
     LX = lx;
   }
+  // frees everything (the workspace of a batch worker ends with its thread)
+  void release() {
+    if (dX) cudaFree(dX);
+    if (dsm) cudaFree(dsm);
+    if (hsm) cudaFreeHost(hsm);
+    if (dpart) cudaFree(dpart);
+    if (dtmp) cudaFree(dtmp);
+    if (own_stream && st) cudaStreamDestroy(st);
+    dX = dsm = hsm = dpart = dtmp = nullptr;
+    st = nullptr;
+    own_stream = false;
+    cap_x = cap_tmp = cap_part = 0;
+  }
   ~Workspace() {}
 };
 

@@ -11,6 +11,8 @@
 // Reverse communication (DPJDREVCOM/DJDREVCOM and the _GEP forms) runs the
 // solver on a worker thread that hands each matvec / preconditioner request
 // back to the caller's thread; all CUDA work stays on the worker.
+#include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -517,6 +519,7 @@ template <class T> struct Global {
   double t_factor = 0, t_upload = 0;
   long n_precond = 0, n_matvec = 0;
   int last_levels = 0, last_fdepth = 0, last_bdepth = 0;
+  int factor_threads = 0;  // host threads of the factorisation (0: all, at most 16)
   void cleanup1() {
     factdgl = 0;
     F = IldlcFactor<H>();
@@ -525,10 +528,24 @@ template <class T> struct Global {
     free_factor(Fb);
     if (ddiag) { cudaFree(ddiag); ddiag = nullptr; }
   }
+  void release() {
+    cleanup1();
+    free_sell(A);
+    free_sell(Bm);
+    resident = false;
+    W.release();
+  }
 };
+// The solver state of an arithmetic: one per process (the reference's COMMON
+// blocks) unless the calling thread installed its own (batch workers).
+template <class T> Global<T>*& thread_global() {
+  static thread_local Global<T>* p = nullptr;
+  return p;
+}
 template <class T> Global<T>& G() {
   static Global<T> g;
-  return g;
+  Global<T>* p = thread_global<T>();
+  return p ? *p : g;
 }
 
 template <class H> static void diag_first(int n, int* ia, int* ja, H* a) {
@@ -702,6 +719,7 @@ int pjdinit(Global<T>& g, Printer& P, int n, typename HostOf<T>::type* a, int* j
     prm.mem = MEM;
     prm.depth_weight = g_opt.depth_weight;
     prm.droptol_schur = g_opt.drop_schur;
+    prm.threads = g.factor_threads;
     double tf0 = wall();
     int ierr = ildlc_factor<H>(n, ia, ja, a, g.shift0, gep ? ib : nullptr, gep ? jb : nullptr, gep ? b : nullptr,
                                prm, g.F);
@@ -1901,6 +1919,53 @@ JDG_API void jdgpu_reset_stats(void) {
   g.t_factor = g.t_upload = 0;
   g.n_precond = g.n_matvec = 0;
   g.nfactor = 0;
+}
+
+
+// Batched DPJD (see the header): worker threads, each with its own solver
+// state and CUDA stream, take problems largest first.
+JDG_API int jdgpu_dpjd_batch(int nprob, const int* n, double* const* a, int* const* ja, int* const* ia,
+                             double* const* eigs, double* const* res, double* const* x, const int* lx, int* neig,
+                             int* iter, int* info, double* gap, double sigma, int isearch, int madspace, double tol,
+                             double droptol, double mem, const int* icntl, int nworkers) {
+  if (nprob < 0 || nworkers < 1 || !n || !a || !ja || !ia || !eigs || !res || !x || !lx || !neig || !iter || !info ||
+      !icntl)
+    return -1;
+  std::vector<int> order(nprob);
+  for (int q = 0; q < nprob; ++q) order[q] = q;
+  std::stable_sort(order.begin(), order.end(), [&](int u, int v) { return n[u] > n[v]; });
+  const int nw = std::max(1, std::min(nworkers, nprob));
+  const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+  const int ft = std::max(1, hw / nw);
+  std::atomic<int> next{0};
+  auto work = [&]() {
+    Global<double> own;
+    own.factor_threads = ft;
+    thread_global<double>() = &own;
+    for (;;) {
+      const int p = next.fetch_add(1);
+      if (p >= nprob) break;
+      const int q = order[p];
+      int N = n[q], LX = lx[q], NEIG = neig[q], ISEARCH = isearch, NINIT = 0, MAD = madspace, ITER = iter[q];
+      int IPRINT = 0, INFO = 0;
+      int ICN[5] = {icntl[0], 0, icntl[2], icntl[3], icntl[4]};
+      double SIGMA = sigma, TOL = tol, SHIFT = 0, DT = droptol, MEM = mem, GAP = 0;
+      pjd_entry<double>(&N, a[q], ja[q], ia[q], nullptr, nullptr, nullptr, eigs[q], res[q], x[q], &LX, &NEIG, &SIGMA,
+                        &ISEARCH, &NINIT, &MAD, &ITER, &TOL, &SHIFT, &DT, &MEM, ICN, &IPRINT, &INFO, &GAP, false);
+      neig[q] = NEIG;
+      iter[q] = ITER;
+      info[q] = INFO;
+      if (gap) gap[q] = GAP;
+      own.cleanup1();
+    }
+    own.release();
+    thread_global<double>() = nullptr;
+  };
+  std::vector<std::thread> th;
+  for (int w = 1; w < nw; ++w) th.emplace_back(work);
+  work();
+  for (auto& t : th) t.join();
+  return 0;
 }
 
 }  // extern "C"

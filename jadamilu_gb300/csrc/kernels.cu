@@ -8,6 +8,8 @@
 // the launch).
 #include <atomic>
 
+#include <mutex>
+
 #include "kernels.cuh"
 
 namespace jdg {
@@ -569,7 +571,9 @@ __global__ void tri_reduce_kernel(int m, const int* __restrict__ irow, const A* 
 // raise the dynamic shared-memory limit of the tail kernel once per size
 // (done before any graph capture: ildl_apply_graph calls it first)
 template <class S, class A> static void ensure_tail_smem(size_t bytes) {
+  static std::mutex mu;
   static size_t set = 48 * 1024;
+  std::lock_guard<std::mutex> lk(mu);
   if (bytes > set) {
     CK(cudaFuncSetAttribute(tail_run_kernel<S, A>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
     set = bytes;
