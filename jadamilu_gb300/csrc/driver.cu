@@ -116,7 +116,7 @@ template <class S> void free_factor(DevFactor<S>& F) {
   void* ps[] = {F.orig, F.lp,  F.li,  F.lx,  F.up,  F.ui,  F.ux,    F.brows, F.blk,   F.partner, F.dv,
                 F.dof,  F.av,  F.aof, F.y,   F.dfptr, F.dbptr, F.rhs_in, F.sol_out, F.tep, F.tei, F.tev,
                 F.tip,  F.tii, F.tiv, F.dtfptr, F.tbp, F.tbi, F.tbv, F.dtbptr, F.tbrows,
-                F.part};
+                F.part, F.xb};
   for (void* p : ps)
     if (p) cudaFree(p);
   for (auto& B : F.blocks) {
@@ -465,24 +465,20 @@ void upload_factor(const IldlcFactor<H>& F, DevFactor<S>& D, cudaStream_t st, Al
       std::vector<S> tf, tb;
       tail_inverse<H, S>(B.m, ip, ii, iv, tf, tb, nth, [](const H& v) { return StoreOf<S>::f(v); });
       B.nt = (B.m + kTile - 1) / kTile;
-      const int64_t ntiles = (int64_t)B.nt * (B.nt + 1) / 2;
-      const int chunk = (int)std::max<int64_t>(1, std::min<int64_t>(16, ntiles / (152 * 8)));
-      TileItems itf = make_items(B.nt, true, chunk), itb = make_items(B.nt, false, chunk);
+      const std::vector<int> itf = make_cluster_items(B.nt, true, 8), itb = make_cluster_items(B.nt, false, 8);
       up_(B.tf, tf);
       up_(B.tb, tb);
-      up_(B.itf, itf.item);
-      up_(B.itb, itb.item);
-      up_(B.irf, itf.irow);
-      up_(B.irb, itb.irow);
-      B.nitf = (int)(itf.item.size() / 4);
-      B.nitb = (int)(itb.item.size() / 4);
-      max_items = std::max(max_items, (size_t)std::max(B.nitf, B.nitb));
+      up_(B.itf, itf);
+      up_(B.itb, itb);
+      B.nitf = (int)(itf.size() / 4);
+      B.nitb = (int)(itb.size() / 4);
+      max_items = std::max(max_items, (size_t)B.m);
       D.tile_bytes += 2.0 * (double)tf.size() * sizeof(S);
     }
     CK(cudaStreamSynchronize(st));  // the host vectors of this block are released next
     D.blocks.push_back(B);
   }
-  if (max_items > 0) D.part = (A*)alloc(sizeof(A) * 64 * max_items);
+  if (max_items > 0) D.xb = (A*)alloc(sizeof(A) * max_items);
   D.y = (A*)alloc(sizeof(A) * std::max(1, n));
   D.rhs_in = alloc(sizeof(zc) * std::max(1, n));
   D.sol_out = alloc(sizeof(zc) * std::max(1, n));

@@ -10,6 +10,8 @@
 
 #include <mutex>
 
+#include <cooperative_groups.h>
+
 #include "kernels.cuh"
 
 namespace jdg {
@@ -370,10 +372,11 @@ __global__ void __launch_bounds__(WIDE_TPB) ildl_wide_kernel(int lo, int hi, con
 
 // Rows [s0, s0 + m) of a block: y[s0 + t] -= sum of row t's entries (local
 // row pointers, global columns), LANES lanes per row.
+// out[t] = y[s0 + t] - sum of row t's entries (out may be y + s0).
 template <class S, class A, int LANES>
 __global__ void __launch_bounds__(WIDE_TPB) tail_ext_kernel(int m, int s_tail, const int64_t* __restrict__ rp,
                                                            const int* __restrict__ ci, const S* __restrict__ cv,
-                                                           A* __restrict__ y) {
+                                                           const A* y, A* out) {
   pdl_begin();
   const int t = blockIdx.x * (WIDE_TPB / LANES) + (threadIdx.x / LANES);
   const int lane = threadIdx.x % LANES;
@@ -381,7 +384,7 @@ __global__ void __launch_bounds__(WIDE_TPB) tail_ext_kernel(int m, int s_tail, c
   if (t < m)
     for (int64_t q = rp[t] + lane; q < rp[t + 1]; q += LANES) acc = fma_(ld_arith(cv + q), y[ci[q]], acc);
   for (int o = LANES / 2; o > 0; o >>= 1) acc = acc + shfl_xor_any(acc, o);
-  if (t < m && lane == 0) y[s_tail + t] = y[s_tail + t] - acc;
+  if (t < m && lane == 0) out[t] = y[s_tail + t] - acc;
 }
 template <class S, class A>
 static void launch_wide(int lanes, int lo, int hi, const int* rows, const int64_t* rp, const int* ci, const S* cv, A* y,
@@ -392,11 +395,13 @@ static void launch_wide(int lanes, int lo, int hi, const int* rows, const int64_
   else launch_k(ildl_wide_kernel<S, A, 8>, dim3(nb), dim3(WIDE_TPB), 0, s, lo, hi, rows, rp, ci, cv, y);
 }
 template <class S, class A>
-static void launch_ext(int lanes, int m, int s0, const int64_t* rp, const int* ci, const S* cv, A* y, cudaStream_t s) {
+static void launch_ext(int lanes, int m, int s0, const int64_t* rp, const int* ci, const S* cv, A* y, A* out,
+                       cudaStream_t s) {
   const int nb = m * lanes / WIDE_TPB + 1;
-  if (lanes == 32) launch_k(tail_ext_kernel<S, A, 32>, dim3(nb), dim3(WIDE_TPB), 0, s, m, s0, rp, ci, cv, y);
-  else if (lanes == 16) launch_k(tail_ext_kernel<S, A, 16>, dim3(nb), dim3(WIDE_TPB), 0, s, m, s0, rp, ci, cv, y);
-  else launch_k(tail_ext_kernel<S, A, 8>, dim3(nb), dim3(WIDE_TPB), 0, s, m, s0, rp, ci, cv, y);
+  const A* yc = y;
+  if (lanes == 32) launch_k(tail_ext_kernel<S, A, 32>, dim3(nb), dim3(WIDE_TPB), 0, s, m, s0, rp, ci, cv, yc, out);
+  else if (lanes == 16) launch_k(tail_ext_kernel<S, A, 16>, dim3(nb), dim3(WIDE_TPB), 0, s, m, s0, rp, ci, cv, yc, out);
+  else launch_k(tail_ext_kernel<S, A, 8>, dim3(nb), dim3(WIDE_TPB), 0, s, m, s0, rp, ci, cv, yc, out);
 }
 // The sequential part of a tail sweep in one CTA.  Shared memory holds the
 // tail of y (yt), the row pointers relative to the first tail entry, the level
@@ -504,32 +509,32 @@ __global__ void __launch_bounds__(RUN_TPB) tail_run_kernel(int m, int s_tail, in
   for (int t = threadIdx.x; t < m; t += RUN_TPB) y[s_tail + t] = yt[t];
 }
 
-// Dense tail product  out = T x  over a set of 64 x 64 tiles (column-major
-// inside a tile).  One CTA per work item {tile row, first tile, tile count,
-// first tile column}: the item's slice of x goes to shared memory, every
-// thread streams 16-byte vectors of V consecutive rows of one tile column,
-// and the per-column partial sums are added in a fixed order, so results do
-// not depend on timing.  tri_reduce_kernel adds the items of each tile row
-// (in order) and writes the result.
-constexpr int TRI_TPB = 256, TRI_CH = 16;
+constexpr int TRI_TPB = 256;  // threads per CTA of the tile kernel
+
+// Dense block product y = T x over a set of 64 x 64 tiles (column-major
+// inside a tile), with the reduction inside a thread-block cluster: the
+// TRI_CL CTAs of a cluster share one tile row and each streams a contiguous
+// chunk of its tiles (16-byte vectors of V consecutive rows of one tile
+// column per thread; per-column partial sums added in a fixed order) into a
+// 64-vector in its shared memory.  Rank 0 adds the TRI_CL vectors in rank
+// order through distributed shared memory and writes the row, so results do
+// not depend on timing.  x must not alias y.
+constexpr int TRI_CL = 8;
 template <class S, class A>
-__global__ void __launch_bounds__(TRI_TPB) tri_partial_kernel(const int4* __restrict__ items,
-                                                             const S* __restrict__ tiles, const A* __restrict__ x,
-                                                             int m, A* __restrict__ part) {
+__global__ void __cluster_dims__(TRI_CL, 1, 1) __launch_bounds__(TRI_TPB)
+    tri_cluster_kernel(const int4* __restrict__ items, const S* __restrict__ tiles, const A* __restrict__ x, int m,
+                       A* __restrict__ y) {
   pdl_begin();
-  constexpr int V = 16 / sizeof(S);   // elements per 16-byte vector
-  constexpr int RG = 64 / V;          // vectors per tile column
-  constexpr int CPS = TRI_TPB / RG;   // tile columns covered by one pass of the CTA
-  constexpr int NS = 64 / CPS;        // passes per tile
-  __shared__ A xs[TRI_CH * 64];
+  namespace cg = cooperative_groups;
+  cg::cluster_group cl = cg::this_cluster();
+  constexpr int V = 16 / sizeof(S);
+  constexpr int RG = 64 / V;
+  constexpr int CPS = TRI_TPB / RG;
+  constexpr int NS = 64 / CPS;
   __shared__ A red[CPS][64];
+  __shared__ A mine[64];
   const int4 it = items[blockIdx.x];
-  const int cnt = it.z, col0 = it.w * 64;
-  for (int t = threadIdx.x; t < cnt * 64; t += TRI_TPB) {
-    const int c = col0 + t;
-    xs[t] = c < m ? x[c] : A(0);
-  }
-  __syncthreads();
+  const int cnt = it.z;
   const int rg = threadIdx.x % RG, cs = threadIdx.x / RG;
   A acc[V];
 #pragma unroll
@@ -541,7 +546,8 @@ __global__ void __launch_bounds__(TRI_TPB) tri_partial_kernel(const int4* __rest
     for (int sl = 0; sl < NS; ++sl) buf[sl] = __ldg(tp + (size_t)k * (64 * 64 / V) + (sl * CPS + cs) * RG + rg);
 #pragma unroll
     for (int sl = 0; sl < NS; ++sl) {
-      const A xv = xs[k * 64 + sl * CPS + cs];
+      const int c = (it.w + k) * 64 + sl * CPS + cs;
+      const A xv = c < m ? x[c] : A(0);
       const S* e = reinterpret_cast<const S*>(&buf[sl]);
 #pragma unroll
       for (int v = 0; v < V; ++v) acc[v] = fma_(ld_arith(e + v), xv, acc[v]);
@@ -554,18 +560,17 @@ __global__ void __launch_bounds__(TRI_TPB) tri_partial_kernel(const int4* __rest
     A sum = red[0][threadIdx.x];
 #pragma unroll
     for (int j = 1; j < CPS; ++j) sum = sum + red[j][threadIdx.x];
-    part[(size_t)blockIdx.x * 64 + threadIdx.x] = sum;
+    mine[threadIdx.x] = sum;
   }
-}
-template <class A>
-__global__ void tri_reduce_kernel(int m, const int* __restrict__ irow, const A* __restrict__ part, A* __restrict__ y) {
-  pdl_begin();
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= m) return;
-  const int i = e >> 6, r = e & 63;
-  A sum = A(0);
-  for (int q = irow[i]; q < irow[i + 1]; ++q) sum = sum + part[(size_t)q * 64 + r];
-  y[e] = sum;
+  cl.sync();
+  if (cl.block_rank() == 0 && threadIdx.x < 64) {
+    A sum = A(0);
+#pragma unroll
+    for (int r = 0; r < TRI_CL; ++r) sum = sum + *cl.map_shared_rank(&mine[threadIdx.x], r);
+    const int e = it.x * 64 + threadIdx.x;
+    if (e < m) y[e] = sum;
+  }
+  cl.sync();  // the other ranks' shared memory stays alive until rank 0 has read it
 }
 
 // raise the dynamic shared-memory limit of the tail kernel once per size
@@ -653,8 +658,8 @@ template <class T, class S> void ildl_apply(const DevFactor<S>& F, bool spd, con
   };
   sweep(F.fseg, F.fptr, F.dfptr, nullptr, F.lp, F.li, F.lx);
   const bool dense = !F.blocks.empty(), levels = F.m_tail > 0 && !dense;
-  auto ext = [&](int m, int s0, const int64_t* rp, const int* ci, const S* cv, int64_t entries) {
-    launch_ext<S, A>(lanes_for((double)entries / std::max(1, m)), m, s0, rp, ci, cv, F.y, s);
+  auto ext = [&](int m, int s0, const int64_t* rp, const int* ci, const S* cv, int64_t entries, A* out) {
+    launch_ext<S, A>(lanes_for((double)entries / std::max(1, m)), m, s0, rp, ci, cv, F.y, out, s);
   };
   const size_t tsm = levels ? std::max(tail_smem_bytes<A>(F.m_tail, (int)F.tfptr.size() - 1, false),
                                        tail_smem_bytes<A>(F.m_tail, (int)F.tbptr.size() - 1, true))
@@ -663,14 +668,17 @@ template <class T, class S> void ildl_apply(const DevFactor<S>& F, bool spd, con
   if (dense) {
     for (const auto& B : F.blocks) {
       A* yb = F.y + B.s0;
-      if (B.nfe > 0) ext(B.m, B.s0, B.ep, B.ei, B.ev, B.nfe);
       if (B.nt > 0) {
-        launch_k(tri_partial_kernel<S, A>, dim3(B.nitf), dim3(TRI_TPB), 0, s, (const int4*)B.itf, B.tf, yb, B.m, F.part);
-        launch_k(tri_reduce_kernel<A>, dim3(nblk(B.m)), dim3(TPB), 0, s, B.m, B.irf, F.part, yb);
+        // right-hand side into xb, then y_B = T xb
+        ext(B.m, B.s0, B.ep, B.ei, B.ev, B.nfe, F.xb);
+        launch_k(tri_cluster_kernel<S, A>, dim3(B.nitf), dim3(TRI_TPB), 0, s, (const int4*)B.itf, B.tf,
+                 (const A*)F.xb, B.m, yb);
+      } else if (B.nfe > 0) {
+        ext(B.m, B.s0, B.ep, B.ei, B.ev, B.nfe, yb);
       }
     }
   } else if (levels) {
-    ext(F.m_tail, F.s_tail, F.tep, F.tei, F.tev, 8 * (int64_t)F.m_tail);
+    ext(F.m_tail, F.s_tail, F.tep, F.tei, F.tev, 8 * (int64_t)F.m_tail, F.y + F.s_tail);
     launch_k(tail_run_kernel<S, A>, dim3(1), dim3(RUN_TPB), tsm, s, F.m_tail, F.s_tail, (int)F.tfptr.size() - 1, F.dtfptr, nullptr,
                                                  F.tip, F.tii, F.tiv, F.y);
   }
@@ -679,10 +687,12 @@ template <class T, class S> void ildl_apply(const DevFactor<S>& F, bool spd, con
     for (auto it = F.blocks.rbegin(); it != F.blocks.rend(); ++it) {
       const auto& B = *it;
       A* yb = F.y + B.s0;
-      if (B.nbe > 0) ext(B.m, B.s0, B.bp, B.bi, B.bv, B.nbe);
       if (B.nt > 0) {
-        launch_k(tri_partial_kernel<S, A>, dim3(B.nitb), dim3(TRI_TPB), 0, s, (const int4*)B.itb, B.tb, yb, B.m, F.part);
-        launch_k(tri_reduce_kernel<A>, dim3(nblk(B.m)), dim3(TPB), 0, s, B.m, B.irb, F.part, yb);
+        ext(B.m, B.s0, B.bp, B.bi, B.bv, B.nbe, F.xb);
+        launch_k(tri_cluster_kernel<S, A>, dim3(B.nitb), dim3(TRI_TPB), 0, s, (const int4*)B.itb, B.tb,
+                 (const A*)F.xb, B.m, yb);
+      } else if (B.nbe > 0) {
+        ext(B.m, B.s0, B.bp, B.bi, B.bv, B.nbe, yb);
       }
     }
   } else if (levels) {

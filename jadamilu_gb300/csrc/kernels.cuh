@@ -73,6 +73,7 @@ template <class S> struct DevFactor {
   // block (DenseBlk) instead of by the single-CTA tail kernels.
   std::vector<DenseBlk<S>> blocks;
   A* part = nullptr;                         // per-item partial sums (64 each)
+  A* xb = nullptr;                           // right-hand side of the dense block being solved
   int64_t sweep_entries = 0;                 // L / L^H entries the two level sweeps read
   double tile_bytes = 0;                     // bytes of both tile sets
   cudaGraphExec_t graph[2] = {nullptr, nullptr};

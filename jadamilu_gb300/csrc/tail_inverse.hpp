@@ -30,23 +30,24 @@ inline std::complex<double> conj_h(const std::complex<double>& v) { return std::
 inline int64_t lower_tile_offset(int I) { return (int64_t)I * (I + 1) / 2; }
 inline int64_t upper_tile_offset(int J, int nt) { return (int64_t)J * nt - (int64_t)J * (J - 1) / 2; }
 
-// Work items of the tiled product: {tile row, first tile (storage index),
-// tile count, first tile column}; rows split into chunks of at most `chunk`
-// tiles.  irow[i]..irow[i+1] are the items of tile row i.
-struct TileItems {
-  std::vector<int> item;  // 4 ints per item
-  std::vector<int> irow;
-};
-inline TileItems make_items(int nt, bool lower, int chunk) {
-  TileItems T;
-  T.irow.push_back(0);
+// Work items of the tile kernel, 4 ints each: {tile row, first tile (storage
+// index), tile count, first tile column}.  Every tile row gets exactly
+// `per_row` items (one thread-block cluster), each with a contiguous chunk of
+// the row's tiles (some chunks may be empty); the item of cluster rank r of
+// row i is item i * per_row + r.
+inline std::vector<int> make_cluster_items(int nt, bool lower, int per_row) {
+  std::vector<int> item;
+  item.reserve((size_t)nt * per_row * 4);
   for (int i = 0; i < nt; ++i) {
     const int c0 = lower ? 0 : i, cnt = lower ? i + 1 : nt - i;
     const int64_t off = lower ? lower_tile_offset(i) : upper_tile_offset(i, nt);
-    for (int k = 0; k < cnt; k += chunk) T.item.insert(T.item.end(), {i, (int)(off + k), std::min(chunk, cnt - k), c0 + k});
-    T.irow.push_back((int)(T.item.size() / 4));
+    const int chunk = (cnt + per_row - 1) / per_row;
+    for (int r = 0; r < per_row; ++r) {
+      const int k0 = std::min(cnt, r * chunk), k1 = std::min(cnt, k0 + chunk);
+      item.insert(item.end(), {i, (int)(off + k0), k1 - k0, c0 + k0});
+    }
   }
-  return T;
+  return item;
 }
 
 // rp/ci/cv: rows t = 0..m-1 of L_TT without the unit diagonal, columns local
