@@ -383,7 +383,8 @@ def run_gb300(args):
                        "madspace": w["kw"]["madspace"], "icntl": [0, -1, 0, 0, args.precision],
                        "factor_s": st["factor_s"], "first_solve_with_factor_s": first_s,
                        "fill": st["fill"], "nnz_l": st["nnz_l"], "levels": st["levels"],
-                       "fwd_depth": st["fwd_depth"], "matvec_per_solve": int(np.median(iters)),
+                       "fwd_depth": st["fwd_depth"], "dense_rows": st["dense_rows"],
+                       "dense_blocks": st["dense_blocks"], "matvec_per_solve": int(np.median(iters)),
                        "parallelism": f"replicas x{world}", "l2": "working set > L2 (no flush needed)",
                        "eigs_min_max": [float(eigs[0]), float(eigs[-1])], "converged": ok,
                        "eigs": [float(v) for v in eigs],

@@ -220,16 +220,20 @@ JDG_API int jdgpu_dpjd_batch(int nprob, const int* n, double* const* a, int* con
  * depth, default 64), "verbose", "dense_tail" (1: solve the deepest levels of
  * the preconditioner with the explicit inverse of their block, default; 0:
  * level by level in one CTA), "dense_max" (most rows of that block, default
- * 32768), "drop_schur" (drop tolerance of the Schur-complement fill; negative:
+ * 32768), "dense_min_saving" (modelled seconds per application the dense
+ * blocks must save to be used, default 1e-4), "drop_schur" (drop tolerance of the Schur-complement fill; negative:
  * DROPTOL/10), "apply_graph" (1: jdgpu_dildl_apply replays the captured CUDA
  * graph of the application, as the eigensolver does).  They apply to factors
  * computed after the call. */
 JDG_API void jdgpu_set_option(const char* name, double value);
 
-/* Statistics of the last real solve (10 doubles): factor seconds, upload
- * seconds, preconditioner applications, matvecs, levels, forward depth,
- * backward depth, nnz(L), fill, factorisations. */
+/* Statistics of the last real (d) or complex (z) solve (12 doubles): factor
+ * seconds, upload seconds, preconditioner applications, matvecs, levels,
+ * forward depth, backward depth, nnz(L), fill, factorisations, rows of the
+ * current device factor solved by dense blocks (or the single-CTA tail), and
+ * the number of those blocks. */
 JDG_API void jdgpu_dstats(double* out);
+JDG_API void jdgpu_zstats(double* out);
 JDG_API void jdgpu_reset_stats(void);
 
 #ifdef __cplusplus

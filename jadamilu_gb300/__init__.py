@@ -75,6 +75,7 @@ def load(build_if_missing: bool = True):
     L.jdgpu_dmatrix_info.argtypes = [_P]
     L.jdgpu_set_stream.argtypes = [_P]
     L.jdgpu_dstats.argtypes = [_P]
+    L.jdgpu_zstats.argtypes = [_P]
     L.jdgpu_reset_stats.argtypes = []
     return L
 
@@ -352,11 +353,13 @@ def set_option(name: str, value: float) -> None:
     load().jdgpu_set_option(name.encode(), float(value))
 
 
-def stats() -> dict:
-    out = np.zeros(10, np.float64)
-    load().jdgpu_dstats(_p(out))
+def stats(complex_: bool = False) -> dict:
+    """Statistics of the last real (or complex) solve."""
+    out = np.zeros(12, np.float64)
+    L = load()
+    (L.jdgpu_zstats if complex_ else L.jdgpu_dstats)(_p(out))
     keys = ["factor_s", "upload_s", "n_precond", "n_matvec", "levels", "fwd_depth", "bwd_depth", "nnz_l", "fill",
-            "nfactor"]
+            "nfactor", "dense_rows", "dense_blocks"]
     return dict(zip(keys, out.tolist()))
 
 

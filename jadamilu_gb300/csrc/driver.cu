@@ -134,6 +134,7 @@ struct Options {
   int verbose = 0;
   int dense_tail = 1;          // solve the deepest levels with their explicit inverse
   int dense_max = 32768;       // at most this many rows in the dense tail
+  double dense_min_saving = 100e-6;  // modelled seconds per application the dense blocks must save
   double drop_schur = -1.0;    // IldlcParams::droptol_schur (negative: its default rule)
   int apply_graph = 0;         // jdgpu_dildl_apply through the captured graph
 };
@@ -155,9 +156,10 @@ struct BlockGroup {
   bool dense;
 };
 static std::vector<BlockGroup> plan_dense_blocks(const std::vector<int>& fptr, const std::vector<int64_t>& ent_f,
-                                                 const std::vector<int64_t>& ent_b, size_t elem_bytes, int dense_max) {
+                                                 const std::vector<int64_t>& ent_b, size_t elem_bytes, int dense_max,
+                                                 double min_saving) {
   const int nfl = (int)fptr.size() - 1;
-  const double t_launch = 4e-6, bw = 5.0e12, min_saving = 100e-6;
+  const double t_launch = 4e-6, bw = 5.0e12;
   const double eb = (double)elem_bytes + 4;
   auto c_lev = [&](int l) { return (l > 0 ? 2 : 1) * t_launch + (double)(ent_f[l] + ent_b[l]) * eb / bw; };
   std::vector<double> best(nfl + 1, 0.0);
@@ -283,7 +285,7 @@ void upload_factor(const IldlcFactor<H>& F, DevFactor<S>& D, cudaStream_t st, Al
         ent_f[l] += lp[s + 1] - lp[s];
         ent_b[l] += up[s + 1] - up[s];
       }
-    groups = plan_dense_blocks(fptr, ent_f, ent_b, sizeof(S), g_opt.dense_max);
+    groups = plan_dense_blocks(fptr, ent_f, ent_b, sizeof(S), g_opt.dense_max, g_opt.dense_min_saving);
     if (!groups.empty()) Lt = groups[0].a;
   } else {
     int acc_rows = 0;
@@ -1889,6 +1891,7 @@ JDG_API void jdgpu_set_option(const char* name, double value) {
   if (!std::strcmp(name, "depth_weight")) g_opt.depth_weight = value;
   else if (!std::strcmp(name, "dense_tail")) g_opt.dense_tail = (int)value;
   else if (!std::strcmp(name, "dense_max")) g_opt.dense_max = (int)value;
+  else if (!std::strcmp(name, "dense_min_saving")) g_opt.dense_min_saving = value;
   else if (!std::strcmp(name, "drop_schur")) g_opt.drop_schur = value;
   else if (!std::strcmp(name, "pdl")) k::set_pdl(value != 0);
   else if (!std::strcmp(name, "apply_graph")) g_opt.apply_graph = (int)value;
@@ -1909,6 +1912,26 @@ JDG_API void jdgpu_dstats(double* out) {
   out[7] = (double)g.F.li.size();
   out[8] = g.F.fill();
   out[9] = g.nfactor;
+  out[10] = g.precision == 1 ? g.Fs.m_tail : g.precision == 2 ? g.Fb.m_tail : g.Fd.m_tail;
+  out[11] = (double)(g.precision == 1 ? g.Fs.blocks.size() : g.precision == 2 ? g.Fb.blocks.size()
+                                                                              : g.Fd.blocks.size());
+}
+// the same for the complex solver state
+JDG_API void jdgpu_zstats(double* out) {
+  Global<zc>& g = G<zc>();
+  out[0] = g.t_factor;
+  out[1] = g.t_upload;
+  out[2] = (double)g.n_precond;
+  out[3] = (double)g.n_matvec;
+  out[4] = g.last_levels;
+  out[5] = g.last_fdepth;
+  out[6] = g.last_bdepth;
+  out[7] = (double)g.F.li.size();
+  out[8] = g.F.fill();
+  out[9] = g.nfactor;
+  out[10] = g.precision == 1 ? g.Fs.m_tail : g.precision == 2 ? g.Fb.m_tail : g.Fd.m_tail;
+  out[11] = (double)(g.precision == 1 ? g.Fs.blocks.size() : g.precision == 2 ? g.Fb.blocks.size()
+                                                                              : g.Fd.blocks.size());
 }
 JDG_API void jdgpu_reset_stats(void) {
   Global<double>& g = G<double>();

@@ -152,3 +152,42 @@ def test_legacy_pjd_forces_float64_preconditioner(gpu, kats):
     np.testing.assert_array_equal(r_leg["eigs"], r_f64["eigs"])
     assert r_leg["iter"] == r_f64["iter"]
     np.testing.assert_allclose(r_leg["eigs"], meta["eigenvalues"], rtol=0, atol=1e-12)
+
+
+@pytest.mark.parametrize("precision", [0, 1, 2])
+def test_dense_blocks_every_real_storage(gpu, precision):
+    """Shallow test factors normally stay on the level path; with the dense
+    blocks forced, the float64, float32 and bfloat16 tile kernels solve the
+    Anderson 14^3 problem to the dense solver's eigenvalues."""
+    ia, ja, a = M.anderson3d(14, seed=6)
+    kw = dict(isearch=2, sigma=0.0, madspace=20, maxit=20000, tol=1e-10, droptol=1e-3, icntl=(0, 0, 0, 0, precision))
+    gpu.set_option("dense_min_saving", -1.0)
+    try:
+        r = gpu.dpjd((a, ja, ia), 4, **kw)
+        st = gpu.stats()
+    finally:
+        gpu.set_option("dense_min_saving", 1e-4)
+    assert r["info"] == 0 and r["neig"] == 4
+    assert st["dense_blocks"] >= 1 and st["dense_rows"] > 0
+    w = np.linalg.eigvalsh(M.to_scipy_full(ia, ja, a).toarray())
+    for lam in r["eigs"]:
+        assert np.min(np.abs(w - lam)) <= 1e-9 * max(1.0, abs(lam))
+    assert np.all(r["res"] <= (1e-10 if precision < 2 else 2e-10))
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_dense_blocks_complex_storage(gpu, precision):
+    """The complex128 and complex64 tile kernels (forced dense blocks) on a
+    complex Hermitian tight-binding problem, against the dense solver."""
+    ia, ja, a = M.tight_binding3d(10, seed=3)
+    kw = dict(isearch=0, sigma=0.0, madspace=20, maxit=20000, tol=1e-10, droptol=1e-3, icntl=(0, 0, 0, 0, precision))
+    gpu.set_option("dense_min_saving", -1.0)
+    try:
+        r = gpu.zpjd((a, ja, ia), 4, **kw)
+        st = gpu.stats(complex_=True)
+    finally:
+        gpu.set_option("dense_min_saving", 1e-4)
+    assert r["info"] == 0 and r["neig"] == 4
+    assert st["dense_blocks"] >= 1 and st["dense_rows"] > 0
+    w = np.linalg.eigvalsh(M.to_scipy_full(ia, ja, a).toarray())
+    np.testing.assert_allclose(np.sort(r["eigs"]), w[:4], rtol=1e-9, atol=1e-12)
