@@ -56,6 +56,7 @@ template <class T>
 __global__ void __launch_bounds__(TPB) spmv_sell_kernel(int n, const int64_t* __restrict__ sptr,
                                                         const int* __restrict__ col, const T* __restrict__ val,
                                                         const T* __restrict__ x, T* __restrict__ y) {
+  pdl_begin();
   int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= n) return;
   int sl = r >> 5, lane = r & 31;
@@ -65,30 +66,33 @@ __global__ void __launch_bounds__(TPB) spmv_sell_kernel(int n, const int64_t* __
   y[r] = acc;
 }
 template <class T> void spmv(const SellMatrix<T>& A, const T* x, T* y, cudaStream_t s) {
-  spmv_sell_kernel<T><<<nblk(A.n), TPB, 0, s>>>(A.n, A.sptr, A.col, A.val, x, y);
+  launch_k(spmv_sell_kernel<T>, dim3(nblk(A.n)), dim3(TPB), 0, s, A.n, A.sptr, A.col, A.val, x, y);
   COUNT_LAUNCH();
 }
 
 // -------------------------------------------------------------- BLAS-1 ----
 template <class T> __global__ void axpy_kernel(long n, T a, const T* __restrict__ x, T* __restrict__ y) {
+  pdl_begin();
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
     y[i] = fma_(a, x[i], y[i]);
 }
 template <class T> __global__ void scal_kernel(long n, double a, T* x) {
+  pdl_begin();
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) x[i] = a * x[i];
 }
 template <class T> __global__ void fill_kernel(long n, T v, T* x) {
+  pdl_begin();
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) x[i] = v;
 }
 static inline int grid_1d(long n) { return (int)std::min<long>(nblk(n), 152L * 16); }
 template <class T> void axpy(long n, T a, const T* x, T* y, cudaStream_t s) {
-  if (n > 0) { axpy_kernel<T><<<grid_1d(n), TPB, 0, s>>>(n, a, x, y); COUNT_LAUNCH(); }
+  if (n > 0) { launch_k(axpy_kernel<T>, dim3(grid_1d(n)), dim3(TPB), 0, s, n, a, x, y); COUNT_LAUNCH(); }
 }
 template <class T> void scal(long n, double a, T* x, cudaStream_t s) {
-  if (n > 0) { scal_kernel<T><<<grid_1d(n), TPB, 0, s>>>(n, a, x); COUNT_LAUNCH(); }
+  if (n > 0) { launch_k(scal_kernel<T>, dim3(grid_1d(n)), dim3(TPB), 0, s, n, a, x); COUNT_LAUNCH(); }
 }
 template <class T> void fill(long n, T v, T* x, cudaStream_t s) {
-  if (n > 0) { fill_kernel<T><<<grid_1d(n), TPB, 0, s>>>(n, v, x); COUNT_LAUNCH(); }
+  if (n > 0) { launch_k(fill_kernel<T>, dim3(grid_1d(n)), dim3(TPB), 0, s, n, v, x); COUNT_LAUNCH(); }
 }
 
 // ---------------------------------------------------- reductions (V^H w) ----
@@ -113,6 +117,7 @@ long mdot_partial_size(long n, int k) { return (long)md_grid(n) * ((k + MD_CH - 
 template <class T>
 __global__ void __launch_bounds__(TPB) mdot_partial_kernel(long n, int k, const T* __restrict__ V, long ldv,
                                                            const T* __restrict__ w, T* __restrict__ partial) {
+  pdl_begin();
   const int c0 = blockIdx.y * MD_CH;
   const int nc = min(MD_CH, k - c0);
   T acc[MD_CH];
@@ -141,6 +146,7 @@ __global__ void __launch_bounds__(TPB) mdot_partial_kernel(long n, int k, const 
 }
 template <class T>
 __global__ void __launch_bounds__(TPB) mdot_final_kernel(int g, const T* __restrict__ partial, T* __restrict__ out) {
+  pdl_begin();
   const int c = blockIdx.x;
   T v = T(0);
   for (int q = threadIdx.x; q < g; q += TPB) v += partial[(long)c * g + q];
@@ -158,8 +164,8 @@ template <class T> void mdot(long n, int k, const T* V, long ldv, const T* w, T*
   if (k <= 0) return;
   int g = md_grid(n);
   dim3 grid(g, (k + MD_CH - 1) / MD_CH);
-  mdot_partial_kernel<T><<<grid, TPB, 0, s>>>(n, k, V, ldv, w, partial);
-  mdot_final_kernel<T><<<k, TPB, 0, s>>>(g, partial, out);
+  launch_k(mdot_partial_kernel<T>, dim3(grid), dim3(TPB), 0, s, n, k, V, ldv, w, partial);
+  launch_k(mdot_final_kernel<T>, dim3(k), dim3(TPB), 0, s, g, partial, out);
   g_launches += 2;
 }
 
@@ -170,6 +176,7 @@ template <class T> struct SmallVec { T v[GMV_MAX]; };
 template <class T>
 __global__ void __launch_bounds__(TPB) gemv_dev_kernel(long n, int k, T alpha, const T* __restrict__ V, long ldv,
                                                        const T* __restrict__ y, T beta, T* __restrict__ w) {
+  pdl_begin();
   __shared__ T ys[GMV_MAX];
   if (threadIdx.x < k) ys[threadIdx.x] = y[threadIdx.x];
   __syncthreads();
@@ -183,6 +190,7 @@ __global__ void __launch_bounds__(TPB) gemv_dev_kernel(long n, int k, T alpha, c
 template <class T>
 __global__ void __launch_bounds__(TPB) gemv_val_kernel(long n, int k, T alpha, const T* __restrict__ V, long ldv,
                                                        SmallVec<T> y, T beta, T* __restrict__ w) {
+  pdl_begin();
   for (long i = blockIdx.x * (long)TPB + threadIdx.x; i < n; i += (long)gridDim.x * TPB) {
     T acc = T(0);
     for (int c = 0; c < k; ++c) acc = fma_(V[i + (long)c * ldv], y.v[c], acc);
@@ -200,7 +208,7 @@ void gemv_dev(long n, int k, T alpha, const T* V, long ldv, const T* y, T beta, 
     }
     return;
   }
-  gemv_dev_kernel<T><<<grid_1d(n), TPB, 0, s>>>(n, k, alpha, V, ldv, y, beta, w);
+  launch_k(gemv_dev_kernel<T>, dim3(grid_1d(n)), dim3(TPB), 0, s, n, k, alpha, V, ldv, y, beta, w);
   COUNT_LAUNCH();
 }
 template <class T>
@@ -212,7 +220,7 @@ void gemv_val(long n, int k, T alpha, const T* V, long ldv, const T* yh, T beta,
   }
   SmallVec<T> y;
   for (int c = 0; c < k; ++c) y.v[c] = yh[c];
-  gemv_val_kernel<T><<<grid_1d(n), TPB, 0, s>>>(n, k, alpha, V, ldv, y, beta, w);
+  launch_k(gemv_val_kernel<T>, dim3(grid_1d(n)), dim3(TPB), 0, s, n, k, alpha, V, ldv, y, beta, w);
   COUNT_LAUNCH();
 }
 
@@ -220,6 +228,7 @@ template <class T> struct SmallMat { T q[32 * 32]; };
 template <class T>
 __global__ void __launch_bounds__(TPB) rmult_kernel(long n, int K, int keep, const T* __restrict__ V, long ldv,
                                                     const T* __restrict__ Q, T* __restrict__ out) {
+  pdl_begin();
   __shared__ T qs[32 * 32];
   for (int t = threadIdx.x; t < K * keep; t += TPB) qs[t] = Q[t];
   __syncthreads();
@@ -243,16 +252,17 @@ template <class T> void rmult(long n, int K, int keep, const T* V, long ldv, con
     for (int kk = 0; kk < K; ++kk) q[kk + c * K] = Qh[kk + c * K];
   CK(cudaMemcpyAsync(dq, q.data(), sizeof(T) * K * keep, cudaMemcpyHostToDevice, s));
   CK(cudaStreamSynchronize(s));  // the pageable source must not change before the copy
-  rmult_kernel<T><<<grid_1d(n), TPB, 0, s>>>(n, K, keep, V, ldv, dq, out);
+  launch_k(rmult_kernel<T>, dim3(grid_1d(n)), dim3(TPB), 0, s, n, K, keep, V, ldv, dq, out);
   COUNT_LAUNCH();
 }
 
 template <class T> __global__ void diag_kernel(long n, const double* __restrict__ d, const T* __restrict__ r, T* x) {
+  pdl_begin();
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
     x[i] = d[i] * r[i];
 }
 template <class T> void diagsolve(long n, const double* d, const T* rhs, T* sol, cudaStream_t s) {
-  diag_kernel<T><<<grid_1d(n), TPB, 0, s>>>(n, d, rhs, sol);
+  launch_k(diag_kernel<T>, dim3(grid_1d(n)), dim3(TPB), 0, s, n, d, rhs, sol);
   COUNT_LAUNCH();
 }
 
