@@ -181,6 +181,11 @@ def dpjd_gep(A, B, neig, **kw):
     return _pjd(False, A, neig, B=B, **kw)
 
 
+def zpjd_gep(A, B, neig, **kw):
+    """ZPJD_GEP: A x = lambda B x with complex Hermitian A and Hermitian positive definite B."""
+    return _pjd(True, A, neig, B=B, **kw)
+
+
 def _revcom(complex_, kind, A, neig, matvec, precond=None, sigma=0.0, isearch=0, ninit=0, madspace=20, maxit=1000,
             tol=1e-10, shift=0.0, droptol=1e-3, mem=20.0, icntl=(0, 0, 0, 0, 0), iprint=0, x=None, eigs=None, n=None,
             B=None, bmatvec=None):

@@ -268,9 +268,20 @@ template <class T> struct DevJd {
       for (long c = 0; c < J; ++c) r[c] = te[c];
     }
   }
+  // SOLPROJEP (JDaux.F:3271-3358); the generalized harmonic case solves
+  // NN X = MM (POSV) and takes the right eigenvectors of X (GEEV).
   void solprojep(long J, H* MM, H* NN, long ld, double& theta, double& theta2, double* w, int is, int& info, bool gep) {
     if (is == 2 || is == -2) {
-      if (gep) { info = -99; return; }
+      if (gep) {
+        info = jdd::posv_u(J, NN, ld, MM, ld);
+        if (info) return;
+        jdd::copyv(ld * ld, MM, NN);
+        info = jdd::geev_right(J, NN, ld, w, MM, ld);
+        if (info) return;
+        sortev_host(J, MM, ld, w, is);
+        theta2 = w[1];
+        return;
+      }
       info = jdd::hegv(J, MM, ld, NN, ld, w);
       if (info) return;
       sortev_host(J, MM, ld, w, is);

@@ -15,6 +15,8 @@
 #include <complex>
 #include <cstring>
 #include <numeric>
+#include <limits>
+#include <type_traits>
 #include <vector>
 
 namespace jdd {
@@ -200,6 +202,178 @@ template <class T> int hegv(long J, T* A, long lda, T* B, long ldb, double* w) {
   for (long j = 0; j < J; ++j)
     for (long i = 0; i < J; ++i) A[i + j * lda] = C[i + j * J];
   return info;
+}
+
+// Solve N X = M for the J x J Hermitian positive definite N (upper triangle
+// given) and J right-hand sides M (J x J, ld); M is overwritten by X and N by
+// its Cholesky factor.  Returns 0 or the failing column+1 (POSV semantics).
+template <class T> int posv_u(long J, T* N, long ldn, T* M, long ldm) {
+  herm_full(J, N, ldn);
+  int info = potrf_l(J, N, ldn);
+  if (info) return info;
+  for (long c = 0; c < J; ++c) {
+    T* x = M + c * ldm;
+    for (long i = 0; i < J; ++i) {  // L y = m
+      T s = x[i];
+      for (long k = 0; k < i; ++k) s -= N[i + k * ldn] * x[k];
+      x[i] = s / N[i + i * ldn];
+    }
+    for (long i = J - 1; i >= 0; --i) {  // L^H x = y
+      T s = x[i];
+      for (long k = i + 1; k < J; ++k) s -= cj(N[k + i * ldn]) * x[k];
+      x[i] = s / N[i + i * ldn];
+    }
+  }
+  return 0;
+}
+
+// Eigenvalues and right eigenvectors of a general J x J matrix A (ld), in
+// complex arithmetic: Householder reduction to Hessenberg form, single-shift
+// QR sweeps (Wilkinson shift from the trailing 2 x 2 block, an exceptional
+// shift after 10 sweeps without deflation) to the triangular Schur form
+// T = Q^H A Q, eigenvectors of T by back substitution, back to A by Q.
+// Each eigenvector is scaled to unit 2-norm with its largest component real
+// (the GEEV convention).  wr receives the real parts of the eigenvalues
+// (unsorted); V (ld) the eigenvectors (real parts for real T).  Returns 0, or
+// 1 when the QR sweeps do not converge.
+template <class T> int geev_right(long J, const T* A, long lda, double* wr, T* V, long ldv) {
+  using Z = std::complex<double>;
+  std::vector<Z> H((size_t)J * J), Q((size_t)J * J, Z(0));
+  auto h = [&](long i, long j) -> Z& { return H[i + j * J]; };
+  auto q = [&](long i, long j) -> Z& { return Q[i + j * J]; };
+  for (long j = 0; j < J; ++j)
+    for (long i = 0; i < J; ++i) h(i, j) = Z(A[i + j * lda]);
+  for (long i = 0; i < J; ++i) q(i, i) = Z(1);
+  // Hessenberg reduction: reflector P = I - 2 v v^H / (v^H v) zeroes column k below k+1
+  for (long k = 0; k + 2 < J; ++k) {
+    double nrm = 0;
+    for (long i = k + 1; i < J; ++i) nrm += std::norm(h(i, k));
+    nrm = std::sqrt(nrm);
+    if (nrm == 0) continue;
+    std::vector<Z> v(J, Z(0));
+    const Z a = h(k + 1, k);
+    const Z ph = std::abs(a) > 0 ? a / std::abs(a) : Z(1);
+    v[k + 1] = a + ph * nrm;
+    for (long i = k + 2; i < J; ++i) v[i] = h(i, k);
+    double vv = 0;
+    for (long i = k + 1; i < J; ++i) vv += std::norm(v[i]);
+    if (vv == 0) continue;
+    for (long j = 0; j < J; ++j) {  // H := P H
+      Z s = 0;
+      for (long i = k + 1; i < J; ++i) s += std::conj(v[i]) * h(i, j);
+      s *= 2.0 / vv;
+      for (long i = k + 1; i < J; ++i) h(i, j) -= v[i] * s;
+    }
+    for (long i = 0; i < J; ++i) {  // H := H P, Q := Q P
+      Z s = 0, t = 0;
+      for (long j = k + 1; j < J; ++j) {
+        s += h(i, j) * v[j];
+        t += q(i, j) * v[j];
+      }
+      s *= 2.0 / vv;
+      t *= 2.0 / vv;
+      for (long j = k + 1; j < J; ++j) {
+        h(i, j) -= s * std::conj(v[j]);
+        q(i, j) -= t * std::conj(v[j]);
+      }
+    }
+    for (long i = k + 2; i < J; ++i) h(i, k) = 0;
+  }
+  double anorm = 0;
+  for (long j = 0; j < J; ++j)
+    for (long i = 0; i < J; ++i) anorm = std::max(anorm, std::abs(h(i, j)));
+  const double eps = std::numeric_limits<double>::epsilon();
+  // shifted QR on the active window [lo, hi]
+  long hi = J - 1;
+  int stall = 0, total = 0;
+  while (hi > 0) {
+    long lo = hi;
+    while (lo > 0) {
+      const double sub = std::abs(h(lo, lo - 1));
+      const double dia = std::abs(h(lo, lo)) + std::abs(h(lo - 1, lo - 1));
+      if (sub <= eps * (dia > 0 ? dia : anorm)) {
+        h(lo, lo - 1) = 0;
+        break;
+      }
+      --lo;
+    }
+    if (lo == hi) {  // one eigenvalue deflated
+      --hi;
+      stall = 0;
+      continue;
+    }
+    if (++total > 60 * J) return 1;
+    // Wilkinson shift: eigenvalue of the trailing 2 x 2 block closer to h(hi, hi)
+    Z mu;
+    if (++stall % 11 == 10) {
+      mu = h(hi, hi) + Z(std::abs(h(hi, hi - 1)) * 0.75, 0);
+    } else {
+      const Z a = h(hi - 1, hi - 1), b = h(hi - 1, hi), c = h(hi, hi - 1), d = h(hi, hi);
+      const Z tr = a + d, det = a * d - b * c;
+      const Z disc = std::sqrt(tr * tr * 0.25 - det);
+      const Z l1 = tr * 0.5 + disc, l2 = tr * 0.5 - disc;
+      mu = std::abs(l1 - d) < std::abs(l2 - d) ? l1 : l2;
+    }
+    // one QR sweep on H(lo:hi, lo:hi) - mu I by Givens rotations (bulge chase)
+    Z x = h(lo, lo) - mu, y = h(lo + 1, lo);
+    for (long k = lo; k < hi; ++k) {
+      const double r = std::sqrt(std::norm(x) + std::norm(y));
+      const Z cs = r > 0 ? x / r : Z(1), sn = r > 0 ? y / r : Z(0);
+      // G = [conj(cs) conj(sn); -sn cs] applied to rows k, k+1 (columns from max(lo, k-1))
+      for (long j = std::max(lo, k - 1); j < J; ++j) {
+        const Z u = h(k, j), w = h(k + 1, j);
+        h(k, j) = std::conj(cs) * u + std::conj(sn) * w;
+        h(k + 1, j) = -sn * u + cs * w;
+      }
+      // columns k, k+1 with G^H (rows up to min(hi, k+2)); accumulate Q
+      for (long i = 0; i <= std::min(hi, k + 2); ++i) {
+        const Z u = h(i, k), w = h(i, k + 1);
+        h(i, k) = u * cs + w * sn;
+        h(i, k + 1) = -u * std::conj(sn) + w * std::conj(cs);
+      }
+      for (long i = 0; i < J; ++i) {
+        const Z u = q(i, k), w = q(i, k + 1);
+        q(i, k) = u * cs + w * sn;
+        q(i, k + 1) = -u * std::conj(sn) + w * std::conj(cs);
+      }
+      if (k + 1 < hi) {
+        x = h(k + 1, k);
+        y = h(k + 2, k);
+      }
+    }
+  }
+  // eigenvectors of the triangular T = H, then V = Q Z
+  std::vector<Z> zv(J), col(J);
+  for (long k = 0; k < J; ++k) {
+    const Z lam = h(k, k);
+    std::fill(zv.begin(), zv.end(), Z(0));
+    zv[k] = Z(1);
+    for (long i = k - 1; i >= 0; --i) {
+      Z s = 0;
+      for (long j = i + 1; j <= k; ++j) s += h(i, j) * zv[j];
+      Z den = h(i, i) - lam;
+      if (std::abs(den) < eps * anorm) den = Z(eps * std::max(anorm, 1e-300), 0);
+      zv[i] = -s / den;
+    }
+    double nrm = 0;
+    long imax = 0;
+    for (long i = 0; i < J; ++i) {
+      Z s = 0;
+      for (long j = 0; j <= k; ++j) s += q(i, j) * zv[j];
+      col[i] = s;
+      nrm += std::norm(s);
+      if (std::abs(s) > std::abs(col[imax])) imax = i;
+    }
+    nrm = std::sqrt(nrm);
+    const Z ph = std::abs(col[imax]) > 0 ? std::conj(col[imax]) / std::abs(col[imax]) : Z(1);
+    for (long i = 0; i < J; ++i) {
+      const Z c = col[i] * ph / nrm;
+      if constexpr (std::is_same<T, double>::value) V[i + k * ldv] = c.real();
+      else V[i + k * ldv] = T(c);
+    }
+    wr[k] = lam.real();
+  }
+  return 0;
 }
 
 // Householder QR of the K x J matrix U (ld); returns the explicit K x K

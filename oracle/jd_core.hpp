@@ -133,12 +133,24 @@ template <class T> struct JdCore {
     }
   }
 
-  // SOLPROJEP: J x J projected eigenproblem.  |is|=2: harmonic (generalized
-  // MM y = mu NN y, sorted by decreasing |mu|); otherwise standard on MM.
-  // is = 3 writes all eigenvalues into NN's first column.
+  // SOLPROJEP (JDaux.F:3271-3358): J x J projected eigenproblem.  |is|=2:
+  // harmonic, sorted by decreasing |mu| -- generalized Hermitian MM y = mu NN y
+  // for the standard problem; for the generalized problem MM is a general
+  // matrix: NN^{-1} MM (Cholesky solve, POSV) and its right eigenvectors
+  // (GEEV), real parts of the eigenvalues.  Otherwise standard on MM.  is = 3
+  // writes all eigenvalues into NN's first column.
   void solprojep(long J, T* MM, T* NN, long ld, double& theta, double& theta2, double* w, int is, int& info, bool gep) {
     if (is == 2 || is == -2) {
-      if (gep) { info = -99; return; }  // POSV+GEEV path: not provided by the oracle
+      if (gep) {
+        info = posv_u(J, NN, ld, MM, ld);
+        if (info) return;
+        copyv(ld * ld, MM, NN);
+        info = geev_right(J, NN, ld, w, MM, ld);
+        if (info) return;
+        sortev(J, J, MM, ld, NN, ld, w, nullptr, is, 0.0);
+        theta2 = w[1];
+        return;
+      }
       info = hegv(J, MM, ld, NN, ld, w);
       if (info) return;
       sortev(J, J, MM, ld, NN, ld, w, nullptr, is, 0.0);

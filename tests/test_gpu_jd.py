@@ -191,3 +191,38 @@ def test_dense_blocks_complex_storage(gpu, precision):
     assert st["dense_blocks"] >= 1 and st["dense_rows"] > 0
     w = np.linalg.eigvalsh(M.to_scipy_full(ia, ja, a).toarray())
     np.testing.assert_allclose(np.sort(r["eigs"]), w[:4], rtol=1e-9, atol=1e-12)
+
+
+def test_generalized_harmonic_interior(gpu, oracle):
+    """DPJD_GEP with ISEARCH = 2 on the GPU: the eigenvalues of K x = lambda M x
+    closest to an interior target, as the dense solver and the oracle give."""
+    import scipy.linalg as sl
+    K, Mm = M.fem_p1(24, seed=3)
+    w = sl.eigh(M.to_scipy_full(*K).toarray(), M.to_scipy_full(*Mm).toarray(), eigvals_only=True)
+    sigma = 0.5 * (w[7] + w[8])
+    ref = np.sort(w[np.argsort(np.abs(w - sigma))[:5]])
+    kw = dict(isearch=2, sigma=sigma, madspace=20, maxit=4000, tol=1e-9, droptol=1e-3)
+    r = gpu.dpjd_gep((K[2], K[1], K[0]), (Mm[2], Mm[1], Mm[0]), 5, **kw)
+    assert r["info"] == 0 and r["neig"] == 5
+    np.testing.assert_allclose(np.sort(r["eigs"]), ref, rtol=1e-10)
+    ro = oracle.dpjd(*K, 5, b=Mm, **kw)
+    np.testing.assert_allclose(np.sort(r["eigs"]), np.sort(ro["eigs"]), rtol=1e-10)
+
+
+def test_generalized_harmonic_complex(gpu):
+    """ZPJD_GEP with ISEARCH = 2: complex Hermitian A, diagonal positive B."""
+    import scipy.linalg as sl
+    ia, ja, a = M.tight_binding3d(8, seed=4)
+    n = len(ia) - 1
+    bdiag = 1.0 + 0.5 * np.random.default_rng(9).uniform(size=n)
+    ib = np.arange(1, n + 2, dtype=np.int32)
+    jb = np.arange(1, n + 1, dtype=np.int32)
+    b = bdiag.astype(np.complex128)
+    Ad = M.to_scipy_full(ia, ja, a).toarray()
+    w = sl.eigh(Ad, np.diag(bdiag), eigvals_only=True)
+    sigma = 0.5 * (w[n // 2] + w[n // 2 + 1])
+    ref = np.sort(w[np.argsort(np.abs(w - sigma))[:4]])
+    r = gpu.zpjd_gep((a, ja, ia), (b, jb, ib), 4, isearch=2, sigma=sigma, madspace=20, maxit=6000, tol=1e-9,
+                     droptol=1e-3)
+    assert r["info"] == 0 and r["neig"] == 4
+    np.testing.assert_allclose(np.sort(r["eigs"]), ref, rtol=1e-9, atol=1e-12)

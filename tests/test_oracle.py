@@ -116,3 +116,17 @@ def test_info_codes(oracle, case, info):
     p = lambda v: v.ctypes.data_as(C.c_void_p)
     L.orc_djd(n, p(E), p(R), p(X), lx, p(NEIG), 0.0, 0, 0, mad, p(ITER), tol, p(INFO), p(GAP), 0, None, None, None)
     assert INFO[0] == info
+
+
+@pytest.mark.parametrize("m,neig", [(16, 4), (24, 5)])
+def test_generalized_harmonic_interior(oracle, m, neig):
+    """K x = lambda M x with ISEARCH = 2 (SOLPROJEP's POSV + GEEV branch):
+    the eigenvalues closest to an interior target."""
+    import scipy.linalg as sl
+    K, Mm = M.fem_p1(m, seed=3)
+    w = sl.eigh(M.to_scipy_full(*K).toarray(), M.to_scipy_full(*Mm).toarray(), eigvals_only=True)
+    sigma = 0.5 * (w[7] + w[8])
+    ref = np.sort(w[np.argsort(np.abs(w - sigma))[:neig]])
+    r = oracle.dpjd(*K, neig, b=Mm, isearch=2, sigma=sigma, madspace=20, maxit=4000, tol=1e-9, droptol=1e-3)
+    assert r["info"] == 0 and r["neig"] == neig
+    np.testing.assert_allclose(np.sort(r["eigs"]), ref, rtol=1e-10)
