@@ -199,6 +199,22 @@ JDG_API int jdgpu_dildl_apply_noalloc(int n, const int* ia, const int* ja, const
 JDG_API int jdgpu_deig_grad(int n, const int* ia, const int* ja, int neig, const double* X, int ldx,
                             const double* w, const double* bdiag, double* grad);
 
+/* Gradient of a loss L(x) of one eigenvector with respect to every stored
+ * entry of A: x an eigenvector of A x = lambda B x (B = I, or diagonal with
+ * diagonal bdiag; NULL for I), any scale; g = dL/dx at x scaled to
+ * x^T B x = 1.  The adjoint mu solves P^T (A - lambda B) P mu = P^T g with
+ * P = I - x x^T B (mu B-orthogonal to x) by preconditioned MINRES on the GPU,
+ * reusing the SpMV and the ILDLC preconditioner (factor of A - lambda B with
+ * DROPTOL droptol, |D| form); stopping at residual tol (relative) or maxit
+ * iterations.  grad[q] for stored entry q (i, j): -(mu_i x_j + mu_j x_i), and
+ * -mu_i x_i on the diagonal (B held fixed; lambda simple).  out (2, may be
+ * NULL): iterations, relative residual.  An extension with no counterpart in
+ * the reference.  Returns 0, a factorisation error code, -1 on bad arguments,
+ * or -99 on a CUDA error. */
+JDG_API int jdgpu_deigvec_grad(int n, const int* ia, const int* ja, const double* a, const double* bdiag,
+                               double lambda, const double* x, const double* g, double droptol, double tol,
+                               int maxit, double* grad, double* out);
+
 /* Batched DPJD: nprob independent real symmetric problems solved by
  * nworkers host threads, each with its own solver state and CUDA stream, so
  * several solves run on the GPU at once; problems are taken largest first.

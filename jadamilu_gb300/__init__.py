@@ -354,6 +354,28 @@ def eig_grad(A, X, w=None, bdiag=None):
     return g
 
 
+def eigvec_grad(A, lam, x, g, bdiag=None, droptol=1e-3, tol=1e-12, maxit=2000):
+    """Gradient of a loss of one eigenvector x (A x = lam B x) with respect to
+    the stored entries of A = (a, ja, ia); g = dL/dx at x scaled to
+    x^T B x = 1 (jdgpu_deigvec_grad).  Returns (grad, iterations, residual)."""
+    L = load()
+    _require_gpu(L)
+    a, ja, ia = _matrix(A, np.float64)
+    n = len(ia) - 1
+    x = np.ascontiguousarray(x, np.float64)
+    g = np.ascontiguousarray(g, np.float64)
+    bd = None if bdiag is None else np.ascontiguousarray(bdiag, np.float64)
+    grad = np.zeros(len(a))
+    out = np.zeros(2)
+    L.jdgpu_deigvec_grad.argtypes = [C.c_int, _P, _P, _P, _P, C.c_double, _P, _P, C.c_double, C.c_double, C.c_int,
+                                     _P, _P]
+    r = L.jdgpu_deigvec_grad(n, _p(ia), _p(ja), _p(a), _p(bd) if bd is not None else None, lam, _p(x), _p(g),
+                             droptol, tol, maxit, _p(grad), _p(out))
+    if r != 0:
+        raise RuntimeError(f"jdgpu_deigvec_grad failed ({r})")
+    return grad, int(out[0]), float(out[1])
+
+
 def set_option(name: str, value: float) -> None:
     load().jdgpu_set_option(name.encode(), float(value))
 

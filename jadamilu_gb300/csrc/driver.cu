@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <limits>
 #include <condition_variable>
 #include <cstring>
 #include <memory>
@@ -1940,6 +1941,167 @@ JDG_API void jdgpu_reset_stats(void) {
   g.nfactor = 0;
 }
 
+
+// Eigenvector-loss gradient (see the header).  The adjoint mu solves
+//   P^T (A - lambda B) P mu = P^T g,  P = I - x x^T B,  x^T B mu = 0,
+// by preconditioned MINRES (Paige and Saunders' recurrences) with the
+// operator and the preconditioner P |L D L^T|^{-1} P^T applied on the GPU:
+// the SELL SpMV, B diagonal, and the ILDLC factor of A - lambda B in its
+// positive definite |D| form.  grad[q] = -(mu_i x_j + mu_j x_i) for a stored
+// off-diagonal entry (i, j), -mu_i x_i on the diagonal.
+JDG_API int jdgpu_deigvec_grad(int n, const int* ia, const int* ja, const double* a, const double* bdiag,
+                               double lambda, const double* xin, const double* g, double droptol, double tol,
+                               int maxit, double* grad, double* out) {
+  if (n <= 1 || !ia || !ja || !a || !xin || !g || !grad || maxit < 1) return -1;
+  try {
+    cudaStream_t st;
+    CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    SellMatrix<double> Am;
+    build_sell<double>(n, ia, ja, a, Am, st);
+    IldlcParams p;
+    p.droptol = droptol;
+    p.condest = 5;
+    p.mem = 0;
+    p.depth_weight = g_opt.depth_weight;
+    p.droptol_schur = g_opt.drop_schur;
+    IldlcFactor<double> F;
+    int ierr;
+    if (bdiag) {  // A - lambda B with B diagonal: B as its own diagonal CSR
+      std::vector<int> ib(n + 1), jb(n);
+      for (int i = 0; i <= n; ++i) ib[i] = i + 1;
+      for (int i = 0; i < n; ++i) jb[i] = i + 1;
+      ierr = ildlc_factor<double>(n, ia, ja, a, lambda, ib.data(), jb.data(), bdiag, p, F);
+    } else {
+      ierr = ildlc_factor<double>(n, ia, ja, a, lambda, nullptr, nullptr, nullptr, p, F);
+    }
+    if (ierr) {
+      free_sell(Am);
+      cudaStreamDestroy(st);
+      return ierr;
+    }
+    DevFactor<double> D;
+    upload_factor(F, D, st);
+    const size_t vb = sizeof(double) * n;
+    enum { X, BX, G, R1, R2, Y, V, W, W1, W2, MU, T1, T2, BD, NV };
+    std::vector<double*> vec(NV, nullptr);
+    for (int k = 0; k < NV; ++k) CK(cudaMalloc(&vec[k], vb));
+    double *dsm, *dpart;
+    CK(cudaMalloc(&dsm, sizeof(double) * 4));
+    CK(cudaMalloc(&dpart, sizeof(double) * k::mdot_partial_size(n, 1)));
+    CK(cudaMemcpyAsync(vec[X], xin, vb, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(vec[G], g, vb, cudaMemcpyHostToDevice, st));
+    if (bdiag) CK(cudaMemcpyAsync(vec[BD], bdiag, vb, cudaMemcpyHostToDevice, st));
+    auto dot = [&](const double* u, const double* w) {
+      double h = 0;
+      k::mdot<double>(n, 1, u, n, w, dsm, dpart, st);
+      CK(cudaMemcpyAsync(&h, dsm, sizeof(double), cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
+      return h;
+    };
+    auto bmul = [&](const double* u, double* w) {  // w = B u
+      if (bdiag) k::diagsolve<double>(n, vec[BD], u, w, st);
+      else CK(cudaMemcpyAsync(w, u, vb, cudaMemcpyDeviceToDevice, st));
+    };
+    // normalise x to x^T B x = 1 (the scale the formula assumes)
+    bmul(vec[X], vec[BX]);
+    const double xbx = dot(vec[X], vec[BX]);
+    if (!(xbx > 0)) throw std::runtime_error("x^T B x is not positive");
+    k::scal<double>(n, 1 / std::sqrt(xbx), vec[X], st);
+    k::scal<double>(n, 1 / std::sqrt(xbx), vec[BX], st);
+    auto proj_t = [&](double* u) {  // u := P^T u = u - B x (x^T u)
+      const double c = dot(vec[X], u);
+      k::axpy<double>(n, -c, vec[BX], u, st);
+    };
+    auto proj = [&](double* u) {  // u := P u = u - x (x^T B u)
+      const double c = dot(vec[BX], u);
+      k::axpy<double>(n, -c, vec[X], u, st);
+    };
+    auto op = [&](const double* u, double* w) {  // w = P^T (A - lambda B) P u
+      CK(cudaMemcpyAsync(vec[T1], u, vb, cudaMemcpyDeviceToDevice, st));
+      proj(vec[T1]);
+      k::spmv<double>(Am, vec[T1], w, st);
+      bmul(vec[T1], vec[T2]);
+      k::axpy<double>(n, -lambda, vec[T2], w, st);
+      proj_t(w);
+    };
+    auto prec = [&](const double* u, double* w) {  // w = P |F|^{-1} P^T u
+      CK(cudaMemcpyAsync(vec[T1], u, vb, cudaMemcpyDeviceToDevice, st));
+      proj_t(vec[T1]);
+      k::ildl_apply<double, double>(D, true, vec[T1], w, st);
+      proj(w);
+    };
+    // preconditioned MINRES from mu = 0 on b = P^T g
+    CK(cudaMemcpyAsync(vec[R1], vec[G], vb, cudaMemcpyDeviceToDevice, st));
+    proj_t(vec[R1]);
+    CK(cudaMemcpyAsync(vec[R2], vec[R1], vb, cudaMemcpyDeviceToDevice, st));
+    prec(vec[R1], vec[Y]);
+    double beta1 = dot(vec[R1], vec[Y]);
+    if (beta1 < 0) throw std::runtime_error("the preconditioner is not positive definite");
+    beta1 = std::sqrt(beta1);
+    for (int k2 : {W, W1, W2, MU}) k::fill<double>(n, 0.0, vec[k2], st);
+    double oldb = 0, beta = beta1, dbar = 0, epsln = 0, phibar = beta1, cs = -1, sn = 0, rnorm = beta1;
+    int it = 0;
+    const double eps = std::numeric_limits<double>::epsilon();
+    while (beta1 > 0 && it < maxit) {
+      ++it;
+      CK(cudaMemcpyAsync(vec[V], vec[Y], vb, cudaMemcpyDeviceToDevice, st));
+      k::scal<double>(n, 1 / beta, vec[V], st);
+      op(vec[V], vec[Y]);
+      if (it >= 2) k::axpy<double>(n, -beta / oldb, vec[R1], vec[Y], st);
+      const double alfa = dot(vec[V], vec[Y]);
+      k::axpy<double>(n, -alfa / beta, vec[R2], vec[Y], st);
+      std::swap(vec[R1], vec[R2]);
+      CK(cudaMemcpyAsync(vec[R2], vec[Y], vb, cudaMemcpyDeviceToDevice, st));
+      prec(vec[R2], vec[Y]);
+      oldb = beta;
+      const double bb = dot(vec[R2], vec[Y]);
+      if (bb < 0) throw std::runtime_error("the preconditioner is not positive definite");
+      beta = std::sqrt(bb);
+      const double oldeps = epsln, delta = cs * dbar + sn * alfa, gbar = sn * dbar - cs * alfa;
+      epsln = sn * beta;
+      dbar = -cs * beta;
+      const double gamma = std::max(std::sqrt(gbar * gbar + beta * beta), eps);
+      cs = gbar / gamma;
+      sn = beta / gamma;
+      const double phi = cs * phibar;
+      phibar = sn * phibar;
+      // w = (v - oldeps w1 - delta w2) / gamma, with w1 <- w2 <- w
+      std::swap(vec[W1], vec[W2]);
+      std::swap(vec[W2], vec[W]);
+      CK(cudaMemcpyAsync(vec[W], vec[V], vb, cudaMemcpyDeviceToDevice, st));
+      k::axpy<double>(n, -oldeps, vec[W1], vec[W], st);
+      k::axpy<double>(n, -delta, vec[W2], vec[W], st);
+      k::scal<double>(n, 1 / gamma, vec[W], st);
+      k::axpy<double>(n, phi, vec[W], vec[MU], st);
+      rnorm = phibar;
+      if (rnorm <= tol * beta1 || beta == 0) break;
+    }
+    proj(vec[MU]);
+    std::vector<double> mu(n), x(n);
+    CK(cudaMemcpyAsync(mu.data(), vec[MU], vb, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(x.data(), vec[X], vb, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    for (int i = 0; i < n; ++i)
+      for (int q = ia[i] - 1; q < ia[i + 1] - 1; ++q) {
+        const int j = ja[q] - 1;
+        grad[q] = (i == j) ? -mu[i] * x[i] : -(mu[i] * x[j] + mu[j] * x[i]);
+      }
+    if (out) {
+      out[0] = it;
+      out[1] = beta1 > 0 ? rnorm / beta1 : 0;
+    }
+    for (auto* v : vec) cudaFree(v);
+    cudaFree(dsm);
+    cudaFree(dpart);
+    free_factor(D);
+    free_sell(Am);
+    cudaStreamDestroy(st);
+    return 0;
+  } catch (std::exception& e) {
+    std::fprintf(stderr, "jdgpu_deigvec_grad: %s\n", e.what());
+    return -99;
+  }
+}
 
 // Batched DPJD (see the header): worker threads, each with its own solver
 // state and CUDA stream, take problems largest first.

@@ -62,3 +62,46 @@ def test_eig_grad_of_gpu_eigenpairs_matches_central_differences(gpu):
             fd[t] = (f[0] - f[1]) / (2 * h)
         err = np.max(np.abs(fd - g[qs])) / np.max(np.abs(g))
         assert err <= bound, (h, err)
+
+
+def test_eigvec_loss_grad_matches_central_differences(gpu):
+    """Gradient of L(x) = c^T x for the third eigenvector of the FEM pencil
+    (from the GPU solver), by the adjoint MINRES solve on the GPU, against
+    central differences (step 1e-6) on 20 seeded stored entries of K."""
+    import scipy.linalg as sl
+    K, Mm = M.fem_p1(20, seed=3)
+    md = M.to_scipy_full(*Mm).toarray().diagonal()
+    r = gpu.dpjd_gep((K[2], K[1], K[0]), (Mm[2], Mm[1], Mm[0]), 3, isearch=0, madspace=20, maxit=4000,
+                     tol=1e-11, droptol=1e-3)
+    assert r["info"] == 0 and r["neig"] == 3
+    a, ja, ia = r["a"], r["ja"], r["ia"]
+    order = np.argsort(r["eigs"])
+    lam, x = r["eigs"][order[2]], r["x"][:, order[2]].copy()
+    x /= np.sqrt(x @ (md * x))
+    n = len(ia) - 1
+    c = np.random.default_rng(1).standard_normal(n)
+    grad, its, res = gpu.eigvec_grad((a, ja, ia), lam, x, c, bdiag=md, tol=1e-12, maxit=3000)
+    assert res <= 1e-10, (its, res)
+    Kd = M.to_scipy_full(ia, ja, a).toarray()
+    Bd = np.diag(md)
+    rows = np.repeat(np.arange(n), np.diff(ia))
+    cols = np.asarray(ja) - 1
+
+    def loss(Kmat):
+        w, X = sl.eigh(Kmat, Bd)
+        xx = X[:, 2]
+        return c @ (xx if xx @ (md * x) > 0 else -xx)
+
+    h = 1e-6
+    err = 0.0
+    for q in np.random.default_rng(7).choice(len(a), 20, replace=False):
+        i, j = rows[q], cols[q]
+        f = []
+        for sgn in (1.0, -1.0):
+            Kp = Kd.copy()
+            Kp[i, j] += sgn * h
+            if i != j:
+                Kp[j, i] += sgn * h
+            f.append(loss(Kp))
+        err = max(err, abs((f[0] - f[1]) / (2 * h) - grad[q]))
+    assert err <= 1e-6 * np.abs(grad).max(), err
