@@ -141,6 +141,18 @@ class Clocks:
                 "samples": len(sm)}
 
 
+def max_over_ranks(value, world, device="cpu"):
+    """The largest of `value` over the ranks of the default process group
+    (replicas report the slowest rank); the value itself for one rank."""
+    if world <= 1:
+        return float(value)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def _finite(v):
     """JSON-safe copy: NaN (a figure not measured for this workload) becomes null."""
     if isinstance(v, dict):
@@ -317,11 +329,7 @@ def run_gb300(args):
     ms = e0.elapsed_time(e1) / args.steps
     launches = L.jdgpu_launch_count() - l0
     clk = clocks.stop()
-    ms_t = torch.tensor([ms], device="cuda")
-    if world > 1:
-        import torch.distributed as dist
-        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
-    ms = float(ms_t.item())
+    ms = max_over_ranks(ms, world, device="cuda")
     # the solver's own test (INFO = 0, all pairs returned); the final Rayleigh-Ritz
     # refinement of a converged cluster recomputes RES, which can end slightly
     # above TOL, as in the reference (JDaux.F:2270-2300); max_res reports it
