@@ -239,8 +239,11 @@ JDG_API int jdgpu_dpjd_batch(int nprob, const int* n, double* const* a, int* con
  * 32768), "dense_min_saving" (modelled seconds per application the dense
  * blocks must save to be used, default 1e-4), "drop_schur" (drop tolerance of the Schur-complement fill; negative:
  * DROPTOL/10), "apply_graph" (1: jdgpu_dildl_apply replays the captured CUDA
- * graph of the application, as the eigensolver does).  They apply to factors
- * computed after the call. */
+ * graph of the application, as the eigensolver does), "fuse_inner" (1,
+ * default: with the built-in matvec the inner CG/sQMR iteration keeps its
+ * scalars on the device and synchronises once per iteration, same arithmetic;
+ * 0: one synchronisation per scalar).  They apply to factors computed, and
+ * solves started, after the call. */
 JDG_API void jdgpu_set_option(const char* name, double value);
 
 /* Statistics of the last real (d) or complex (z) solve (12 doubles): factor

@@ -381,12 +381,61 @@ correction:
       if (GEP) fill(N, H(0), BTv);
       int it = 0;
       bool fail = false;
+      // RHO of iteration `it` is kept in device slot kScal + (it & 1), so the
+      // next iteration finds its predecessor there.
+      T* const scd = W->dsm + kScal;
       for (;;) {
         ++it;
+        if (device_ops && it > 1) {
+          // The same operations in the same order, with RHO, the projection
+          // coefficient, P^H Q, B-inner product and |R|^2 left on the
+          // device and read back together: one synchronisation per
+          // iteration.  The checks on RHO and P^H Q come after the read;
+          // a failed check leaves P, Q, Z and R modified where the plain
+          // sequence stops earlier, and none of them is read after a failed
+          // inner solve (it > 1).
+          precond(R, Zv);
+          S_.flagcg = true;
+          repgs(N, UU, BU, NEIG + 1, Zv, nullptr, EPSM, -1);
+          T* rho_d = scd + (it & 1);
+          k::mdot<T>(N, 1, D(R), N, D(Zv), rho_d, W->dpart, S());
+          k::axpy_ratio<T>(N, rho_d, scd + ((it - 1) & 1), 1.0, D(P), D(Zv), S());
+          copy(N, Zv, P);
+          matvec(1, P, Q, Zv);
+          AXPYALPHA = H(-ETA);
+          if (GEP) axpy(N, AXPYALPHA, Zv, Q);
+          else axpy(N, AXPYALPHA, P, Q);
+          if (GEP) k::mdot<T>(N, 1, D(BU), N, D(Q), scd + 4, W->dpart, S());
+          cgs_dev(N, BU, UU, 1, Q, scd + 2);
+          k::mdot<T>(N, 1, D(P), N, D(Q), scd + 3, W->dpart, S());
+          k::axpy_ratio<T>(N, rho_d, scd + 3, -1.0, D(Q), D(R), S());
+          k::mdot<T>(N, 1, D(R), N, D(R), scd + 5, W->dpart, S());
+          CK(cudaMemcpyAsync(W->hsm + kScal, scd, sizeof(T) * 6, cudaMemcpyDeviceToHost, S()));
+          sync();
+          const H* hs = reinterpret_cast<const H*>(W->hsm + kScal);
+          RHO = hre(hs[it & 1]);
+          if (POSDEF && RHO <= 0) {
+            std::fprintf(stderr, " Non fatal bug: the preconditioner is not positive definite\n");
+            fail = true;
+            break;
+          }
+          if (RHO == 0) { fail = true; break; }
+          if (GEP) AXPYALPHA = hs[4] / (NBU * NBU);
+          X[NP] = hs[2];
+          ALPRHO = hre(X[NP]);
+          ITER++;
+          alpha_cg = hre(hs[3]);
+          if ((POSDEF && alpha_cg <= 0) || alpha_cg == 0) { fail = true; break; }
+          alpha_cg = RHO / alpha_cg;
+          GK = std::sqrt(rl(W->hsm[kScal + 5]));
+        } else {
         precond(R, Zv);
         S_.flagcg = true;
         repgs(N, UU, BU, NEIG + 1, Zv, nullptr, EPSM, -1);
-        RHO = hre(dot(N, R, Zv));
+        k::mdot<T>(N, 1, D(R), N, D(Zv), scd + (it & 1), W->dpart, S());
+        CK(cudaMemcpyAsync(W->hsm + kScal, scd + (it & 1), sizeof(T), cudaMemcpyDeviceToHost, S()));
+        sync();
+        RHO = hre(reinterpret_cast<const H*>(W->hsm + kScal)[0]);
         if (POSDEF && RHO <= 0) {
           std::fprintf(stderr, " Non fatal bug: the preconditioner is not positive definite\n");
           fail = true;
@@ -412,6 +461,7 @@ correction:
         alpha_cg = RHO / alpha_cg;
         axpy(N, H(-alpha_cg), Q, R);
         GK = nrm2(N, R);
+        }
         if (GEP) axpy(N, H(alpha_cg), Zv, BTv);
         if (POSDEF) {
           axpy(N, H(alpha_cg), P, Xc);

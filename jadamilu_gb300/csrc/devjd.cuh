@@ -124,6 +124,11 @@ template <class T> struct DevJd {
   double alpha_cg = 0;
   int istag = 0;
   long launches = 0;
+  // The operators are the library's own stream-ordered kernels (no host
+  // round trip inside matvec/precond): the inner iteration may then keep its
+  // scalars on the device and read them back once per iteration.
+  bool device_ops = false;
+  static constexpr int kScal = 500;  // dsm slots of the inner-iteration scalars
 
   T* D(long off) { return W->dX + off; }
   cudaStream_t S() { return W->st; }
@@ -165,6 +170,12 @@ template <class T> struct DevJd {
     }
   }
   void axpy(long n, H a, long x, long y) { k::axpy<T>(n, todev(a), D(x), D(y), S()); }
+  // classical Gram-Schmidt of REPGS (gam < 0) with the coefficients left in
+  // device memory at cdev
+  void cgs_dev(long N, long V, long BV, long JV, long w, T* cdev) {
+    k::mdot<T>(N, (int)JV, D(BV), N, D(w), cdev, W->dpart, S());
+    k::gemv_dev<T>(N, (int)JV, T(-1), D(V), N, cdev, T(1), D(w), S());
+  }
   void scal(long n, double a, long x) { k::scal<T>(n, a, D(x), S()); }
   void copy(long n, long x, long y) {
     if (n > 0 && x != y) CK(cudaMemcpyAsync(D(y), D(x), sizeof(T) * n, cudaMemcpyDeviceToDevice, S()));

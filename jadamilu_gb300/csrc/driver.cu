@@ -138,6 +138,7 @@ struct Options {
   double dense_min_saving = 100e-6;  // modelled seconds per application the dense blocks must save
   double drop_schur = -1.0;    // IldlcParams::droptol_schur (negative: its default rule)
   int apply_graph = 0;         // jdgpu_dildl_apply through the captured graph
+  int fuse_inner = 1;          // inner iterations read their scalars back once (library operators only)
 };
 static Options g_opt;
 
@@ -1037,6 +1038,7 @@ void pjd_drive(int n, typename HostOf<T>::type* a, int* ja, int* ia, typename Ho
   if (user_mv) jd.matvec = user_mv;
   else jd.matvec = [&R](int w, long x, long y, long by) { R.builtin_mv(w, x, y, by); };
   jd.precond = [&R](long r, long s) { R.precond(r, s); };
+  jd.device_ops = !user_mv && g_opt.fuse_inner != 0;
   if (R.P.pr >= 2)
     jd.on_step = [](int conv, int step, int k, double th, double v) {
       if (conv) std::printf("Step:%4d(%3d) ;  #MV:%7d ;  Rayl. quot.:%12.5E * converged\n\n", step, k, (int)v, th);
@@ -1896,6 +1898,7 @@ JDG_API void jdgpu_set_option(const char* name, double value) {
   else if (!std::strcmp(name, "drop_schur")) g_opt.drop_schur = value;
   else if (!std::strcmp(name, "pdl")) k::set_pdl(value != 0);
   else if (!std::strcmp(name, "apply_graph")) g_opt.apply_graph = (int)value;
+  else if (!std::strcmp(name, "fuse_inner")) g_opt.fuse_inner = (int)value;
   else if (!std::strcmp(name, "verbose")) g_opt.verbose = (int)value;
 }
 

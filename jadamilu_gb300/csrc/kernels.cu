@@ -76,6 +76,16 @@ template <class T> __global__ void axpy_kernel(long n, T a, const T* __restrict_
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
     y[i] = fma_(a, x[i], y[i]);
 }
+// y += sign * (Re num / Re den) * x, the two scalars read from device memory
+// (results of earlier reductions on the same stream)
+template <class T>
+__global__ void axpy_ratio_kernel(long n, const T* num, const T* den, double sign, const T* __restrict__ x,
+                                  T* __restrict__ y) {
+  pdl_begin();
+  const T a = T(sign * (rl(*num) / rl(*den)));
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    y[i] = fma_(a, x[i], y[i]);
+}
 template <class T> __global__ void scal_kernel(long n, double a, T* x) {
   pdl_begin();
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) x[i] = a * x[i];
@@ -87,6 +97,10 @@ template <class T> __global__ void fill_kernel(long n, T v, T* x) {
 static inline int grid_1d(long n) { return (int)std::min<long>(nblk(n), 152L * 16); }
 template <class T> void axpy(long n, T a, const T* x, T* y, cudaStream_t s) {
   if (n > 0) { launch_k(axpy_kernel<T>, dim3(grid_1d(n)), dim3(TPB), 0, s, n, a, x, y); COUNT_LAUNCH(); }
+}
+template <class T>
+void axpy_ratio(long n, const T* num, const T* den, double sign, const T* x, T* y, cudaStream_t s) {
+  if (n > 0) { launch_k(axpy_ratio_kernel<T>, dim3(grid_1d(n)), dim3(TPB), 0, s, n, num, den, sign, x, y); COUNT_LAUNCH(); }
 }
 template <class T> void scal(long n, double a, T* x, cudaStream_t s) {
   if (n > 0) { launch_k(scal_kernel<T>, dim3(grid_1d(n)), dim3(TPB), 0, s, n, a, x); COUNT_LAUNCH(); }
@@ -741,6 +755,7 @@ template <class T, class S> void ildl_apply_graph(DevFactor<S>& F, bool spd, con
 #define JD_INST_T(T)                                                                               \
   template void spmv<T>(const SellMatrix<T>&, const T*, T*, cudaStream_t);                         \
   template void axpy<T>(long, T, const T*, T*, cudaStream_t);                                      \
+  template void axpy_ratio<T>(long, const T*, const T*, double, const T*, T*, cudaStream_t);        \
   template void scal<T>(long, double, T*, cudaStream_t);                                           \
   template void fill<T>(long, T, T*, cudaStream_t);                                                \
   template void mdot<T>(long, int, const T*, long, const T*, T*, T*, cudaStream_t);                \

@@ -92,6 +92,8 @@ void add_launches(long long n);
 
 template <class T> void spmv(const SellMatrix<T>& A, const T* x, T* y, cudaStream_t s);
 template <class T> void axpy(long n, T a, const T* x, T* y, cudaStream_t s);
+// y += sign * (Re *num / Re *den) * x with num and den in device memory
+template <class T> void axpy_ratio(long n, const T* num, const T* den, double sign, const T* x, T* y, cudaStream_t s);
 template <class T> void scal(long n, double a, T* x, cudaStream_t s);
 template <class T> void fill(long n, T v, T* x, cudaStream_t s);
 // out[c] = V(:,c)^H w for c < k (deterministic two-pass reduction); partial

@@ -57,13 +57,19 @@ class Factor:
                                _ptr(ierr))
         self.ierr = int(ierr[0])
 
+    def _check(self):
+        if self.ierr != 0:
+            raise RuntimeError(f"factorisation failed: ierr={self.ierr}")
+
     def info(self):
+        self._check()
         out = np.zeros(8, np.int64)
         lib().orc_dfactor_info(self.h, _ptr(out))
         keys = ["n", "nnz_l", "nneg", "nlevels", "fwd_depth", "bwd_depth", "n2x2"]
         return dict(zip(keys, out[:7].tolist()))
 
     def apply(self, b, spd=False, single=False):
+        self._check()
         b = np.ascontiguousarray(b, np.float64)
         x = np.zeros_like(b)
         lib().orc_dfactor_apply(self.h, int(spd), int(single), _ptr(b), _ptr(x))
