@@ -399,12 +399,15 @@ correction:
           repgs(N, UU, BU, NEIG + 1, Zv, nullptr, EPSM, -1);
           T* rho_d = scd + (it & 1);
           k::mdot<T>(N, 1, D(R), N, D(Zv), rho_d, W->dpart, S());
-          k::axpy_ratio<T>(N, rho_d, scd + ((it - 1) & 1), 1.0, D(P), D(Zv), S());
-          copy(N, Zv, P);
-          matvec(1, P, Q, Zv);
+          k::axpy_ratio_copy<T>(N, rho_d, scd + ((it - 1) & 1), D(P), D(Zv), D(P), S());
           AXPYALPHA = H(-ETA);
-          if (GEP) axpy(N, AXPYALPHA, Zv, Q);
-          else axpy(N, AXPYALPHA, P, Q);
+          if (!GEP && matvec_shift) {
+            matvec_shift(P, Q, AXPYALPHA);
+          } else {
+            matvec(1, P, Q, Zv);
+            if (GEP) axpy(N, AXPYALPHA, Zv, Q);
+            else axpy(N, AXPYALPHA, P, Q);
+          }
           if (GEP) k::mdot<T>(N, 1, D(BU), N, D(Q), scd + 4, W->dpart, S());
           cgs_dev(N, BU, UU, 1, Q, scd + 2);
           k::mdot<T>(N, 1, D(P), N, D(Q), scd + 3, W->dpart, S());
@@ -472,9 +475,7 @@ correction:
           double CK2 = 1 / (1 + TTK2);
           GGK2 = GGK2 * TTK2 * CK2;
           if (it > 1) {
-            axpy(N, H(alpha_cg / TTK2M), P, X2);
-            scal(N, TTK2M * CK2, X2);
-            axpy(N, H(1), X2, Xc);
+            k::smooth<T>(N, todev(H(alpha_cg / TTK2M)), D(P), TTK2M * CK2, D(X2), D(Xc), S());
           } else {
             copy(N, P, X2);
             scal(N, alpha_cg * CK2, X2);

@@ -118,6 +118,8 @@ template <class T> struct DevJd {
   // which: 1 = A x (and B x for GEP), 3 = A x, 4 = B x; offsets into X
   std::function<void(int, long, long, long)> matvec;
   std::function<void(long, long)> precond;  // (rhs, sol)
+  // optional y = A x + a x in one pass (built-in matrix, no B)
+  std::function<void(long, long, H)> matvec_shift;
   std::function<void(int, int, int, double, double)> on_step;  // progress printer (may be empty)
   StopStateD<T> st;
   Lcg48d rng;

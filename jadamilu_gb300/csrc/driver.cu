@@ -827,6 +827,10 @@ template <class T> struct PjdRun {
     if (which == 1 || which == 3) k::spmv<T>(g.A, jd.D(x), jd.D(y), g.W.st);
     if ((which == 1 || which == 4) && gep) k::spmv<T>(g.Bm, jd.D(x), jd.D(by), g.W.st);
   }
+  void builtin_mv_shift(long x, long y, typename HostOf<T>::type a) {
+    g.n_matvec++;
+    k::spmv_shift<T>(g.A, todev(a), jd.D(x), jd.D(y), g.W.st);
+  }
   void precond(long rhs, long sol);
 };
 
@@ -1039,6 +1043,8 @@ void pjd_drive(int n, typename HostOf<T>::type* a, int* ja, int* ia, typename Ho
   else jd.matvec = [&R](int w, long x, long y, long by) { R.builtin_mv(w, x, y, by); };
   jd.precond = [&R](long r, long s) { R.precond(r, s); };
   jd.device_ops = !user_mv && g_opt.fuse_inner != 0;
+  if (jd.device_ops && !gep)
+    jd.matvec_shift = [&R](long x, long y, typename HostOf<T>::type a) { R.builtin_mv_shift(x, y, a); };
   if (R.P.pr >= 2)
     jd.on_step = [](int conv, int step, int k, double th, double v) {
       if (conv) std::printf("Step:%4d(%3d) ;  #MV:%7d ;  Rayl. quot.:%12.5E * converged\n\n", step, k, (int)v, th);

@@ -69,6 +69,24 @@ template <class T> void spmv(const SellMatrix<T>& A, const T* x, T* y, cudaStrea
   launch_k(spmv_sell_kernel<T>, dim3(nblk(A.n)), dim3(TPB), 0, s, A.n, A.sptr, A.col, A.val, x, y);
   COUNT_LAUNCH();
 }
+// y = A x + a x: the row sum, then the same fused multiply-add as axpy
+template <class T>
+__global__ void __launch_bounds__(TPB) spmv_shift_kernel(int n, const int64_t* __restrict__ sptr,
+                                                         const int* __restrict__ col, const T* __restrict__ val,
+                                                         T a, const T* __restrict__ x, T* __restrict__ y) {
+  pdl_begin();
+  int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  int sl = r >> 5, lane = r & 31;
+  int64_t b = sptr[sl], e = sptr[sl + 1];
+  T acc = T(0);
+  for (int64_t q = b + lane; q < e; q += 32) acc = fma_(val[q], x[__ldg(col + q)], acc);
+  y[r] = fma_(a, x[r], acc);
+}
+template <class T> void spmv_shift(const SellMatrix<T>& A, T a, const T* x, T* y, cudaStream_t s) {
+  launch_k(spmv_shift_kernel<T>, dim3(nblk(A.n)), dim3(TPB), 0, s, A.n, A.sptr, A.col, A.val, a, x, y);
+  COUNT_LAUNCH();
+}
 
 // -------------------------------------------------------------- BLAS-1 ----
 template <class T> __global__ void axpy_kernel(long n, T a, const T* __restrict__ x, T* __restrict__ y) {
@@ -86,6 +104,27 @@ __global__ void axpy_ratio_kernel(long n, const T* num, const T* den, double sig
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
     y[i] = fma_(a, x[i], y[i]);
 }
+// y += (Re num / Re den) * x, then out = y (out may alias x)
+template <class T>
+__global__ void axpy_ratio_copy_kernel(long n, const T* num, const T* den, const T* x, T* __restrict__ y, T* out) {
+  pdl_begin();
+  const T a = T(1.0 * (rl(*num) / rl(*den)));
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const T t = fma_(a, x[i], y[i]);
+    y[i] = t;
+    out[i] = t;
+  }
+}
+// x2 = s (x2 + a p); xc = x2 + xc, as axpy, scal and axpy in sequence
+template <class T>
+__global__ void smooth_kernel(long n, T a, const T* __restrict__ p, double s, T* __restrict__ x2, T* __restrict__ xc) {
+  pdl_begin();
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const T t = s * fma_(a, p[i], x2[i]);
+    x2[i] = t;
+    xc[i] = fma_(T(1), t, xc[i]);
+  }
+}
 template <class T> __global__ void scal_kernel(long n, double a, T* x) {
   pdl_begin();
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) x[i] = a * x[i];
@@ -101,6 +140,12 @@ template <class T> void axpy(long n, T a, const T* x, T* y, cudaStream_t s) {
 template <class T>
 void axpy_ratio(long n, const T* num, const T* den, double sign, const T* x, T* y, cudaStream_t s) {
   if (n > 0) { launch_k(axpy_ratio_kernel<T>, dim3(grid_1d(n)), dim3(TPB), 0, s, n, num, den, sign, x, y); COUNT_LAUNCH(); }
+}
+template <class T> void axpy_ratio_copy(long n, const T* num, const T* den, const T* x, T* y, T* out, cudaStream_t s) {
+  if (n > 0) { launch_k(axpy_ratio_copy_kernel<T>, dim3(grid_1d(n)), dim3(TPB), 0, s, n, num, den, x, y, out); COUNT_LAUNCH(); }
+}
+template <class T> void smooth(long n, T a, const T* p, double sc, T* x2, T* xc, cudaStream_t s) {
+  if (n > 0) { launch_k(smooth_kernel<T>, dim3(grid_1d(n)), dim3(TPB), 0, s, n, a, p, sc, x2, xc); COUNT_LAUNCH(); }
 }
 template <class T> void scal(long n, double a, T* x, cudaStream_t s) {
   if (n > 0) { launch_k(scal_kernel<T>, dim3(grid_1d(n)), dim3(TPB), 0, s, n, a, x); COUNT_LAUNCH(); }
@@ -126,6 +171,7 @@ static inline int md_grid(long n) {
   if (n < 4096) return (int)std::max<long>(1, (n + 2047) / 2048);
   return (int)std::min<long>((n + 511) / 512, 152L * 8);
 }
+
 long mdot_partial_size(long n, int k) { return (long)md_grid(n) * ((k + MD_CH - 1) / MD_CH) * MD_CH; }
 
 template <class T>
@@ -544,6 +590,15 @@ constexpr int TRI_TPB = 256;  // threads per CTA of the tile kernel
 // order through distributed shared memory and writes the row, so results do
 // not depend on timing.  x must not alias y.
 constexpr int TRI_CL = 8;
+// 16-byte read-only load of data read once per launch (tiles): issued as
+// written, kept in its registers (no re-load at the point of use), no L1 allocation
+__device__ __forceinline__ uint4 ld_stream(const uint4* p) {
+  uint4 r;
+  asm volatile("ld.global.nc.L1::no_allocate.v4.u32 {%0, %1, %2, %3}, [%4];"
+               : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
+               : "l"(p));
+  return r;
+}
 template <class S, class A>
 __global__ void __cluster_dims__(TRI_CL, 1, 1) __launch_bounds__(TRI_TPB)
     tri_cluster_kernel(const int4* __restrict__ items, const S* __restrict__ tiles, const A* __restrict__ x, int m,
@@ -564,10 +619,11 @@ __global__ void __cluster_dims__(TRI_CL, 1, 1) __launch_bounds__(TRI_TPB)
 #pragma unroll
   for (int v = 0; v < V; ++v) acc[v] = A(0);
   const uint4* tp = reinterpret_cast<const uint4*>(tiles) + (size_t)it.y * (64 * 64 / V);
-  for (int k = 0; k < cnt; ++k) {
-    uint4 buf[NS];
+  auto load = [&](int k, uint4* buf) {
 #pragma unroll
-    for (int sl = 0; sl < NS; ++sl) buf[sl] = __ldg(tp + (size_t)k * (64 * 64 / V) + (sl * CPS + cs) * RG + rg);
+    for (int sl = 0; sl < NS; ++sl) buf[sl] = ld_stream(tp + (size_t)k * (64 * 64 / V) + (sl * CPS + cs) * RG + rg);
+  };
+  auto use = [&](int k, const uint4* buf) {
 #pragma unroll
     for (int sl = 0; sl < NS; ++sl) {
       const int c = (it.w + k) * 64 + sl * CPS + cs;
@@ -576,6 +632,15 @@ __global__ void __cluster_dims__(TRI_CL, 1, 1) __launch_bounds__(TRI_TPB)
 #pragma unroll
       for (int v = 0; v < V; ++v) acc[v] = fma_(ld_arith(e + v), xv, acc[v]);
     }
+  };
+  // One tile per step.  Measured on GB300 (fp32 factor, Anderson model,
+  // ms per application): 40^3 0.220 -> 0.198 with these loads instead of
+  // __ldg, 50^3 unchanged; issuing the next tile's loads before the current
+  // tile's products made 50^3 slower (0.387 -> 0.410).
+  for (int k = 0; k < cnt; ++k) {
+    uint4 b0[NS];
+    load(k, b0);
+    use(k, b0);
   }
 #pragma unroll
   for (int v = 0; v < V; ++v) red[cs][V * rg + v] = acc[v];
@@ -756,6 +821,9 @@ template <class T, class S> void ildl_apply_graph(DevFactor<S>& F, bool spd, con
   template void spmv<T>(const SellMatrix<T>&, const T*, T*, cudaStream_t);                         \
   template void axpy<T>(long, T, const T*, T*, cudaStream_t);                                      \
   template void axpy_ratio<T>(long, const T*, const T*, double, const T*, T*, cudaStream_t);        \
+  template void axpy_ratio_copy<T>(long, const T*, const T*, const T*, T*, T*, cudaStream_t);        \
+  template void smooth<T>(long, T, const T*, double, T*, T*, cudaStream_t);                         \
+  template void spmv_shift<T>(const SellMatrix<T>&, T, const T*, T*, cudaStream_t);                 \
   template void scal<T>(long, double, T*, cudaStream_t);                                           \
   template void fill<T>(long, T, T*, cudaStream_t);                                                \
   template void mdot<T>(long, int, const T*, long, const T*, T*, T*, cudaStream_t);                \

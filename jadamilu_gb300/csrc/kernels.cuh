@@ -91,9 +91,15 @@ void set_pdl(bool on);
 void add_launches(long long n);
 
 template <class T> void spmv(const SellMatrix<T>& A, const T* x, T* y, cudaStream_t s);
+// y = A x + a x (the shifted operator of the correction equation)
+template <class T> void spmv_shift(const SellMatrix<T>& A, T a, const T* x, T* y, cudaStream_t s);
 template <class T> void axpy(long n, T a, const T* x, T* y, cudaStream_t s);
 // y += sign * (Re *num / Re *den) * x with num and den in device memory
 template <class T> void axpy_ratio(long n, const T* num, const T* den, double sign, const T* x, T* y, cudaStream_t s);
+// y += (Re *num / Re *den) * x; out = y (out may alias x)
+template <class T> void axpy_ratio_copy(long n, const T* num, const T* den, const T* x, T* y, T* out, cudaStream_t s);
+// x2 = s (x2 + a p); xc += x2 (axpy, scal, axpy with the same roundings)
+template <class T> void smooth(long n, T a, const T* p, double sc, T* x2, T* xc, cudaStream_t s);
 template <class T> void scal(long n, double a, T* x, cudaStream_t s);
 template <class T> void fill(long n, T v, T* x, cudaStream_t s);
 // out[c] = V(:,c)^H w for c < k (deterministic two-pass reduction); partial
