@@ -90,6 +90,43 @@ __device__ __forceinline__ float ld_arith(const float* p) { return *p; }
 __device__ __forceinline__ double ld_arith(const double* p) { return *p; }
 __device__ __forceinline__ cc ld_arith(const cc* p) { return *p; }
 __device__ __forceinline__ zc ld_arith(const zc* p) { return *p; }
+// The same loads for factor entries and column indices streamed once per
+// sweep: read-only path, no L1 allocation (L1 stays for the gathered vector).
+__device__ __forceinline__ float ld_arith_nc(const float* p) {
+  float r;
+  asm("ld.global.nc.L1::no_allocate.f32 %0, [%1];" : "=f"(r) : "l"(p));
+  return r;
+}
+__device__ __forceinline__ double ld_arith_nc(const double* p) {
+  double r;
+  asm("ld.global.nc.L1::no_allocate.f64 %0, [%1];" : "=d"(r) : "l"(p));
+  return r;
+}
+__device__ __forceinline__ float ld_arith_nc(const __nv_bfloat16* p) {
+  unsigned short r;
+  asm("ld.global.nc.L1::no_allocate.b16 %0, [%1];" : "=h"(r) : "l"(p));
+  return __bfloat162float(__ushort_as_bfloat16(r));
+}
+__device__ __forceinline__ cc ld_arith_nc(const cc* p) {
+  float x, y;
+  asm("ld.global.nc.L1::no_allocate.v2.f32 {%0, %1}, [%2];" : "=f"(x), "=f"(y) : "l"(p));
+  return cc(x, y);
+}
+__device__ __forceinline__ zc ld_arith_nc(const zc* p) {
+  double x, y;
+  asm("ld.global.nc.L1::no_allocate.v2.f64 {%0, %1}, [%2];" : "=d"(x), "=d"(y) : "l"(p));
+  return zc(x, y);
+}
+__device__ __forceinline__ cc ld_arith_nc(const bc* p) {
+  unsigned short x, y;
+  asm("ld.global.nc.L1::no_allocate.v2.b16 {%0, %1}, [%2];" : "=h"(x), "=h"(y) : "l"(p));
+  return cc(__bfloat162float(__ushort_as_bfloat16(x)), __bfloat162float(__ushort_as_bfloat16(y)));
+}
+__device__ __forceinline__ int ld_idx_nc(const int* p) {
+  int r;
+  asm("ld.global.nc.L1::no_allocate.s32 %0, [%1];" : "=r"(r) : "l"(p));
+  return r;
+}
 
 inline void cuda_check(cudaError_t e, const char* what) {
   if (e != cudaSuccess) throw std::runtime_error(std::string("CUDA error in ") + what + ": " + cudaGetErrorString(e));

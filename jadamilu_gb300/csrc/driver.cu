@@ -459,6 +459,10 @@ void upload_factor(const IldlcFactor<H>& F, DevFactor<S>& D, cudaStream_t st, Al
     B.nfe = (int64_t)ei.size();
     B.nbe = (int64_t)bi.size();
     D.sweep_entries += B.nfe + B.nbe;
+    if (g_opt.verbose)
+      std::fprintf(stderr, "block rows %d..%d (%d, %s): external entries %lld forward, %lld backward\n", B.s0,
+                   B.s0 + B.m - 1, B.m, gr.dense ? "explicit inverse" : "gather only", (long long)B.nfe,
+                   (long long)B.nbe);
     up_(B.ep, ep);
     up_(B.ei, ei);
     up_(B.ev, ev);

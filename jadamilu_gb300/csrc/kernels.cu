@@ -442,8 +442,12 @@ __global__ void __launch_bounds__(WIDE_TPB) ildl_wide_kernel(int lo, int hi, con
 
 // Rows [s0, s0 + m) of a block: y[s0 + t] -= sum of row t's entries (local
 // row pointers, global columns), LANES lanes per row.
-// out[t] = y[s0 + t] - sum of row t's entries (out may be y + s0).
-template <class S, class A, int LANES>
+// out[t] = y[s0 + t] - sum of row t's entries (out may be y + s0).  NC: the
+// entries and column indices are read without L1 allocation, which keeps L1
+// for the gathered y; measured on GB300 it pays for blocks with a million or
+// more external entries (Anderson 50^3 application 0.387 -> 0.356 ms with it
+// on every block) and costs a little on smaller ones (40^3: 0.198 -> 0.202).
+template <class S, class A, int LANES, bool NC>
 __global__ void __launch_bounds__(WIDE_TPB) tail_ext_kernel(int m, int s_tail, const int64_t* __restrict__ rp,
                                                            const int* __restrict__ ci, const S* __restrict__ cv,
                                                            const A* y, A* out) {
@@ -452,7 +456,10 @@ __global__ void __launch_bounds__(WIDE_TPB) tail_ext_kernel(int m, int s_tail, c
   const int lane = threadIdx.x % LANES;
   A acc = A(0);
   if (t < m)
-    for (int64_t q = rp[t] + lane; q < rp[t + 1]; q += LANES) acc = fma_(ld_arith(cv + q), y[ci[q]], acc);
+    for (int64_t q = rp[t] + lane; q < rp[t + 1]; q += LANES) {
+      if (NC) acc = fma_(ld_arith_nc(cv + q), y[ld_idx_nc(ci + q)], acc);
+      else acc = fma_(ld_arith(cv + q), y[ci[q]], acc);
+    }
   for (int o = LANES / 2; o > 0; o >>= 1) acc = acc + shfl_xor_any(acc, o);
   if (t < m && lane == 0) out[t] = y[s_tail + t] - acc;
 }
@@ -464,14 +471,20 @@ static void launch_wide(int lanes, int lo, int hi, const int* rows, const int64_
   else if (lanes == 16) launch_k(ildl_wide_kernel<S, A, 16>, dim3(nb), dim3(WIDE_TPB), 0, s, lo, hi, rows, rp, ci, cv, y);
   else launch_k(ildl_wide_kernel<S, A, 8>, dim3(nb), dim3(WIDE_TPB), 0, s, lo, hi, rows, rp, ci, cv, y);
 }
+constexpr int64_t kExtStreamEntries = 1 << 20;  // external entries from which tail_ext streams them
+template <class S, class A, bool NC>
+static void launch_ext_(int lanes, int m, int s0, const int64_t* rp, const int* ci, const S* cv, const A* y, A* out,
+                        cudaStream_t s) {
+  const int nb = m * lanes / WIDE_TPB + 1;
+  if (lanes == 32) launch_k(tail_ext_kernel<S, A, 32, NC>, dim3(nb), dim3(WIDE_TPB), 0, s, m, s0, rp, ci, cv, y, out);
+  else if (lanes == 16) launch_k(tail_ext_kernel<S, A, 16, NC>, dim3(nb), dim3(WIDE_TPB), 0, s, m, s0, rp, ci, cv, y, out);
+  else launch_k(tail_ext_kernel<S, A, 8, NC>, dim3(nb), dim3(WIDE_TPB), 0, s, m, s0, rp, ci, cv, y, out);
+}
 template <class S, class A>
 static void launch_ext(int lanes, int m, int s0, const int64_t* rp, const int* ci, const S* cv, A* y, A* out,
-                       cudaStream_t s) {
-  const int nb = m * lanes / WIDE_TPB + 1;
-  const A* yc = y;
-  if (lanes == 32) launch_k(tail_ext_kernel<S, A, 32>, dim3(nb), dim3(WIDE_TPB), 0, s, m, s0, rp, ci, cv, yc, out);
-  else if (lanes == 16) launch_k(tail_ext_kernel<S, A, 16>, dim3(nb), dim3(WIDE_TPB), 0, s, m, s0, rp, ci, cv, yc, out);
-  else launch_k(tail_ext_kernel<S, A, 8>, dim3(nb), dim3(WIDE_TPB), 0, s, m, s0, rp, ci, cv, yc, out);
+                       int64_t entries, cudaStream_t s) {
+  if (entries >= kExtStreamEntries) launch_ext_<S, A, true>(lanes, m, s0, rp, ci, cv, y, out, s);
+  else launch_ext_<S, A, false>(lanes, m, s0, rp, ci, cv, y, out, s);
 }
 // The sequential part of a tail sweep in one CTA.  Shared memory holds the
 // tail of y (yt), the row pointers relative to the first tail entry, the level
@@ -748,7 +761,7 @@ template <class T, class S> void ildl_apply(const DevFactor<S>& F, bool spd, con
   sweep(F.fseg, F.fptr, F.dfptr, nullptr, F.lp, F.li, F.lx);
   const bool dense = !F.blocks.empty(), levels = F.m_tail > 0 && !dense;
   auto ext = [&](int m, int s0, const int64_t* rp, const int* ci, const S* cv, int64_t entries, A* out) {
-    launch_ext<S, A>(lanes_for((double)entries / std::max(1, m)), m, s0, rp, ci, cv, F.y, out, s);
+    launch_ext<S, A>(lanes_for((double)entries / std::max(1, m)), m, s0, rp, ci, cv, F.y, out, entries, s);
   };
   const size_t tsm = levels ? std::max(tail_smem_bytes<A>(F.m_tail, (int)F.tfptr.size() - 1, false),
                                        tail_smem_bytes<A>(F.m_tail, (int)F.tbptr.size() - 1, true))
