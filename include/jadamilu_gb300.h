@@ -242,9 +242,28 @@ JDG_API int jdgpu_dpjd_batch(int nprob, const int* n, double* const* a, int* con
  * graph of the application, as the eigensolver does), "fuse_inner" (1,
  * default: with the built-in matvec the inner CG/sQMR iteration keeps its
  * scalars on the device and synchronises once per iteration, same arithmetic;
- * 0: one synchronisation per scalar).  They apply to factors computed, and
- * solves started, after the call. */
+ * 0: one synchronisation per scalar), "revcom_device" (1: reverse-
+ * communication requests on device pointers, see jdgpu_revcom_device_ptr).
+ * They apply to factors computed, and solves started, after the call. */
 JDG_API void jdgpu_set_option(const char* name, double value);
+
+/* Device-pointer reverse communication (no reference counterpart; extends
+ * DPJDREVCOM / DJDREVCOM and their _GEP and Z forms, src/jd/PJD.F:268-429,
+ * 576-798, for GPU-resident user operators).  With
+ * jdgpu_set_option("revcom_device", 1) before a solve starts (IJOB = 0), its
+ * requests are served on the device copy of X instead of the caller's X:
+ * after a return with IJOB = 1, 2, 3 or 4, jdgpu_revcom_device_ptr gives the
+ * device address XD of X(1) and the solver's CUDA stream; the request reads
+ * XD[NDX1-1 ...] (IJOB 1, 3, 4) or XD[NDX2-1 ...] (IJOB 2) and writes
+ * XD[NDX2-1 ...], XD[NDX3-1 ...] (B x, GEP) or XD[NDX1-1 ...] (IJOB 2), N
+ * entries each, exactly as the host protocol does with X.  The input vectors
+ * are complete when the driver returns; the caller's results must be complete
+ * when it calls the driver again (work enqueued on the returned stream
+ * counts).  The caller's X receives the eigenvectors at the end as usual; it
+ * holds no request vectors in between.  Returns 0, or -1 when no solve of
+ * that arithmetic (complex_ 0: real, 1: complex) is waiting on a
+ * device-mode request. */
+JDG_API int jdgpu_revcom_device_ptr(int complex_, void** xd, void** stream);
 
 /* Statistics of the last real (d) or complex (z) solve (12 doubles): factor
  * seconds, upload seconds, preconditioner applications, matvecs, levels,

@@ -67,6 +67,8 @@ def load(build_if_missing: bool = True):
     L.jdgpu_dildl_apply.argtypes = [C.c_int, _P, _P, _P, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int,
                                     C.c_int, _P, _P, _P]
     L.jdgpu_set_option.argtypes = [C.c_char_p, C.c_double]
+    L.jdgpu_revcom_device_ptr.argtypes = [C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]
+    L.jdgpu_revcom_device_ptr.restype = C.c_int
     L.jdgpu_deig_grad.argtypes = [C.c_int, _P, _P, C.c_int, _P, C.c_int, _P, _P, _P]
     L.jdgpu_dildl_bench.argtypes = [C.c_int, _P, _P, _P, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int,
                                     C.c_int, _P]
@@ -188,10 +190,19 @@ def zpjd_gep(A, B, neig, **kw):
 
 def _revcom(complex_, kind, A, neig, matvec, precond=None, sigma=0.0, isearch=0, ninit=0, madspace=20, maxit=1000,
             tol=1e-10, shift=0.0, droptol=1e-3, mem=20.0, icntl=(0, 0, 0, 0, 0), iprint=0, x=None, eigs=None, n=None,
-            B=None, bmatvec=None):
-    """Reverse-communication loop: serves IJOB requests with Python callables."""
+            B=None, bmatvec=None, device=False):
+    """Reverse-communication loop: serves IJOB requests with Python callables.
+
+    Host mode: ``matvec(x) -> A x``, ``bmatvec(x) -> B x``, ``precond(r) -> z``
+    on numpy vectors.  Device mode (``device=True``, jdgpu_revcom_device_ptr):
+    the callables get device addresses and serve the request on the GPU,
+    ``matvec(x_addr, y_addr, n, stream)``, ``bmatvec(x_addr, y_addr, n, stream)``,
+    ``precond(r_addr, z_addr, n, stream)``; their results must be complete (or
+    enqueued on ``stream``) when they return."""
     L = load()
     _require_gpu(L)
+    item = 16 if complex_ else 8
+    first = True
     dt = np.complex128 if complex_ else np.float64
     pre = "z" if complex_ else "d"
     if A is not None:
@@ -200,10 +211,13 @@ def _revcom(complex_, kind, A, neig, matvec, precond=None, sigma=0.0, isearch=0,
     s = _Args(n, neig, sigma, isearch, ninit, madspace, maxit, tol, shift, droptol, mem, icntl, iprint, dt, x, eigs)
     X = s.X
     gep = B is not None or bmatvec is not None
+    if kind == "pjd" and gep:
+        b, jb, ib = _matrix(B, dt)
     while True:
+        if first and device:  # the mode is taken when the solve starts (IJOB = 0)
+            L.jdgpu_set_option(b"revcom_device", C.c_double(1.0))
         if kind == "pjd":
             if gep:
-                b, jb, ib = _matrix(B, dt)
                 getattr(L, pre + "pjdrevcom_gep_")(
                     _p(s.n), _p(a), _p(ja), _p(ia), _p(b), _p(jb), _p(ib), _p(s.EIGS), _p(s.RES), _p(X), _p(s.lx),
                     _p(s.NEIG), _p(s.SIGMA), _p(s.ISEARCH), _p(s.NINIT), _p(s.MADSPACE), _p(s.ITER), _p(s.TOL),
@@ -226,10 +240,25 @@ def _revcom(complex_, kind, A, neig, matvec, precond=None, sigma=0.0, isearch=0,
                     _p(s.n), _p(s.EIGS), _p(s.RES), _p(X), _p(s.lx), _p(s.NEIG), _p(s.SIGMA), _p(s.ISEARCH),
                     _p(s.NINIT), _p(s.MADSPACE), _p(s.ITER), _p(s.TOL), _p(s.IJOB), _p(s.NDX[0:1]), _p(s.NDX[1:2]),
                     _p(s.IPRINT), _p(s.INFO), _p(s.GAP))
+        if first and device:
+            L.jdgpu_set_option(b"revcom_device", C.c_double(0.0))
+        first = False
         ijob = int(s.IJOB[0])
         if ijob == 0:
             break
         i1, i2, i3 = (int(v) - 1 for v in s.NDX)
+        if device:
+            xd, st = C.c_void_p(), C.c_void_p()
+            if L.jdgpu_revcom_device_ptr(int(complex_), C.byref(xd), C.byref(st)) != 0:
+                raise RuntimeError("no device-mode request pending")
+            base, stream = int(xd.value), int(st.value or 0)
+            if ijob in (1, 3):
+                matvec(base + i1 * item, base + i2 * item, n, stream)
+            if gep and ijob in (1, 4):
+                bmatvec(base + i1 * item, base + i3 * item, n, stream)
+            if ijob == 2:
+                precond(base + i2 * item, base + i1 * item, n, stream)
+            continue
         if ijob in (1, 3):
             X[i2:i2 + n] = matvec(X[i1:i1 + n].copy())
         if gep and ijob in (1, 4):

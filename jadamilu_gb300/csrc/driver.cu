@@ -139,6 +139,7 @@ struct Options {
   double drop_schur = -1.0;    // IldlcParams::droptol_schur (negative: its default rule)
   int apply_graph = 0;         // jdgpu_dildl_apply through the captured graph
   int fuse_inner = 1;          // inner iterations read their scalars back once (library operators only)
+  int revcom_device = 0;       // reverse-communication requests are served on the device copy of X
 };
 static Options g_opt;
 
@@ -1129,6 +1130,7 @@ struct Revcom {
   enum State { IDLE, RUNNING, REQUEST, DONE } state = IDLE;
   int ijob = 0, ndx1 = 0, ndx2 = 0, ndx3 = 0;
   bool cancel = false;
+  bool device = false;  // requests served on the device copy of X
   std::string error;
   // worker side: post a request and wait for the caller to serve it
   void request(int job, long x1, long x2, long x3) {
@@ -1195,14 +1197,24 @@ template <class T> Revcom& RC() {
   return r;
 }
 
-// matvec/precond request wrappers: device <-> caller's X around each request
+// matvec/precond request wrappers: device <-> caller's X around each request,
+// or (device mode) the request is served in place on the device copy of X,
+// whose vectors are complete when the request is posted.
 template <class T>
 std::function<void(int, long, long, long)> revcom_matvec(Revcom& rc, typename HostOf<T>::type* X, bool gep,
-                                                         bool pjd, int n) {
-  return [&rc, X, gep, pjd, n](int which, long x, long y, long by) {
+                                                         bool pjd, int n, bool dev) {
+  return [&rc, X, gep, pjd, n, dev](int which, long x, long y, long by) {
     Global<T>& g = G<T>();
     T* dX = g.W.dX;
     auto st = g.W.st;
+    if (dev) {
+      CK(cudaStreamSynchronize(st));
+      int job = which;
+      if (!gep && job == 3) job = 1;
+      rc.request(job, x, y, by);
+      g.n_matvec++;
+      return;
+    }
     CK(cudaMemcpyAsync(X + x, dX + x, sizeof(T) * n, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     int job = which;
@@ -1216,11 +1228,17 @@ std::function<void(int, long, long, long)> revcom_matvec(Revcom& rc, typename Ho
   };
 }
 template <class T>
-std::function<void(long, long)> revcom_precond(Revcom& rc, typename HostOf<T>::type* X, int n) {
-  return [&rc, X, n](long rhs, long sol) {
+std::function<void(long, long)> revcom_precond(Revcom& rc, typename HostOf<T>::type* X, int n, bool dev) {
+  return [&rc, X, n, dev](long rhs, long sol) {
     Global<T>& g = G<T>();
     T* dX = g.W.dX;
     auto st = g.W.st;
+    if (dev) {
+      CK(cudaStreamSynchronize(st));
+      rc.request(2, sol, rhs, 0);
+      g.n_precond++;
+      return;
+    }
     CK(cudaMemcpyAsync(X + rhs, dX + rhs, sizeof(T) * n, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     rc.request(2, sol, rhs, 0);
@@ -1322,7 +1340,8 @@ void pjdrevcom_entry(int* N, typename HostOf<T>::type* A, int* JA, int* IA, type
                      int* IPRINT, int* INFO, double* GAP, bool gep) {
   Revcom& rc = RC<T>();
   if (*IJOB == 0) {
-    auto mv = revcom_matvec<T>(rc, X, gep, true, *N);
+    rc.device = g_opt.revcom_device != 0;
+    auto mv = revcom_matvec<T>(rc, X, gep, true, *N, rc.device);
     rc.start([=] {
       pjd_drive<T>(*N, A, JA, IA, B, JB, IB, EIGS, RES, X, *LX, NEIG, *SIGMA, *ISEARCH, *NINIT, *MADSPACE, ITER,
                    *TOL, SHIFT, DROPTOL, MEM, ICNTL, *IPRINT, INFO, GAP, gep, mv);
@@ -1347,8 +1366,9 @@ void jdrevcom_entry(int* N, double* EIGS, double* RES, typename HostOf<T>::type*
                     int* NDX3, int* IPRINT, int* INFO, double* GAP, bool gep) {
   Revcom& rc = RC<T>();
   if (*IJOB == 0) {
-    auto mv = revcom_matvec<T>(rc, X, gep, false, *N);
-    auto pc = revcom_precond<T>(rc, X, *N);
+    rc.device = g_opt.revcom_device != 0;
+    auto mv = revcom_matvec<T>(rc, X, gep, false, *N, rc.device);
+    auto pc = revcom_precond<T>(rc, X, *N, rc.device);
     rc.start([=] {
       jd_drive<T>(*N, EIGS, RES, X, *LX, NEIG, *SIGMA, *ISEARCH, *NINIT, *MADSPACE, ITER, *TOL, *IPRINT, INFO, GAP,
                   gep, mv, pc);
@@ -1367,6 +1387,19 @@ void jdrevcom_entry(int* N, double* EIGS, double* RES, typename HostOf<T>::type*
   if (NDX3) *NDX3 = rc.ndx3;
 }
 
+// Device address of X(1) and the stream of the reverse-communication solve
+// that is waiting on a request in device mode (see the header).
+template <class T> int revcom_device_ptr(void** xd, void** stream) {
+  Revcom& rc = RC<T>();
+  {
+    std::lock_guard<std::mutex> lk(rc.m);
+    if (!rc.device || rc.state != Revcom::REQUEST) return -1;
+  }
+  Global<T>& g = G<T>();
+  if (xd) *xd = (void*)g.W.dX;
+  if (stream) *stream = (void*)g.W.st;
+  return 0;
+}
 template <class T> void cleanup_entry() {
   RC<T>().finish_old();
   G<T>().cleanup1();
@@ -1900,6 +1933,10 @@ JDG_API int jdgpu_dildl_apply_noalloc(int n, const int* ia, const int* ja, const
   }
 }
 
+JDG_API int jdgpu_revcom_device_ptr(int complex_, void** xd, void** stream) {
+  return complex_ ? revcom_device_ptr<zc>(xd, stream) : revcom_device_ptr<double>(xd, stream);
+}
+
 JDG_API void jdgpu_set_option(const char* name, double value) {
   if (!std::strcmp(name, "depth_weight")) g_opt.depth_weight = value;
   else if (!std::strcmp(name, "dense_tail")) g_opt.dense_tail = (int)value;
@@ -1909,6 +1946,7 @@ JDG_API void jdgpu_set_option(const char* name, double value) {
   else if (!std::strcmp(name, "pdl")) k::set_pdl(value != 0);
   else if (!std::strcmp(name, "apply_graph")) g_opt.apply_graph = (int)value;
   else if (!std::strcmp(name, "fuse_inner")) g_opt.fuse_inner = (int)value;
+  else if (!std::strcmp(name, "revcom_device")) g_opt.revcom_device = (int)value;
   else if (!std::strcmp(name, "verbose")) g_opt.verbose = (int)value;
 }
 
