@@ -23,10 +23,12 @@
 #ifdef __cplusplus
 #include <complex>
 typedef std::complex<double> jdg_zcomplex;
+typedef std::complex<float> jdg_ccomplex;
 #define JDG_API __attribute__((visibility("default")))
 extern "C" {
 #else
 typedef struct { double re, im; } jdg_zcomplex;
+typedef struct { float re, im; } jdg_ccomplex;
 #define JDG_API
 #endif
 
@@ -113,6 +115,62 @@ JDG_API void zjdrevcom_gep_(int* N, double* EIGS, double* RES, jdg_zcomplex* X, 
 JDG_API void zpjdcleanup_(void);
 
 /* ---- single-kernel entry points (host arrays in and out) ---- */
+
+/* Single-precision drivers: SPJD, SPJD_GEP, SPJDREVCOM, SPJDREVCOM_GEP,
+ * SJDREVCOM, SJDREVCOM_GEP, SPJDCLEANUP (Doc/SPJD_prototypes.f:3-798) and
+ * CPJD ... CPJDCLEANUP (Doc/CPJD_prototypes.f:3-798), which the reference
+ * builds from src/jd/PJD.F with _SINGLE_REAL_ / _SINGLE_COMPLEX_
+ * (src/include/ilupackmacros.h:379-400).  Arguments and protocol as the
+ * double drivers above with REAL (COMPLEX) values.  The iteration runs in
+ * double precision on widened copies of the caller's arrays, with the results
+ * rounded back; reverse-communication requests convert only their vectors.
+ * They share the double drivers' state: an S (C) and a D (Z) reverse-
+ * communication solve cannot be in flight together.  32-bit integers only. */
+JDG_API void spjd_(int* N, float* A, int* JA, int* IA, float* EIGS, float* RES, float* X, int* LX, int* NEIG,
+                   float* SIGMA, int* ISEARCH, int* NINIT, int* MADSPACE, int* ITER, float* TOL, float* SHIFT,
+                   float* DROPTOL, float* MEM, int* ICNTL, int* IPRINT, int* INFO, float* GAP);
+JDG_API void spjd_gep_(int* N, float* A, int* JA, int* IA, float* B, int* JB, int* IB, float* EIGS, float* RES,
+                       float* X, int* LX, int* NEIG, float* SIGMA, int* ISEARCH, int* NINIT, int* MADSPACE, int* ITER,
+                       float* TOL, float* SHIFT, float* DROPTOL, float* MEM, int* ICNTL, int* IPRINT, int* INFO,
+                       float* GAP);
+JDG_API void spjdrevcom_(int* N, float* A, int* JA, int* IA, float* EIGS, float* RES, float* X, int* LX, int* NEIG,
+                         float* SIGMA, int* ISEARCH, int* NINIT, int* MADSPACE, int* ITER, float* TOL, float* SHIFT,
+                         float* DROPTOL, float* MEM, int* ICNTL, int* IJOB, int* NDX1, int* NDX2, int* IPRINT,
+                         int* INFO, float* GAP);
+JDG_API void spjdrevcom_gep_(int* N, float* A, int* JA, int* IA, float* B, int* JB, int* IB, float* EIGS, float* RES,
+                             float* X, int* LX, int* NEIG, float* SIGMA, int* ISEARCH, int* NINIT, int* MADSPACE,
+                             int* ITER, float* TOL, float* SHIFT, float* DROPTOL, float* MEM, int* ICNTL, int* IJOB,
+                             int* NDX1, int* NDX2, int* NDX3, int* IPRINT, int* INFO, float* GAP);
+JDG_API void sjdrevcom_(int* N, float* EIGS, float* RES, float* X, int* LX, int* NEIG, float* SIGMA, int* ISEARCH,
+                        int* NINIT, int* MADSPACE, int* ITER, float* TOL, int* IJOB, int* NDX1, int* NDX2, int* IPRINT,
+                        int* INFO, float* GAP);
+JDG_API void sjdrevcom_gep_(int* N, float* EIGS, float* RES, float* X, int* LX, int* NEIG, float* SIGMA, int* ISEARCH,
+                            int* NINIT, int* MADSPACE, int* ITER, float* TOL, int* IJOB, int* NDX1, int* NDX2,
+                            int* NDX3, int* IPRINT, int* INFO, float* GAP);
+JDG_API void spjdcleanup_(void);
+JDG_API void cpjd_(int* N, jdg_ccomplex* A, int* JA, int* IA, float* EIGS, float* RES, jdg_ccomplex* X, int* LX,
+                   int* NEIG, float* SIGMA, int* ISEARCH, int* NINIT, int* MADSPACE, int* ITER, float* TOL,
+                   float* SHIFT, float* DROPTOL, float* MEM, int* ICNTL, int* IPRINT, int* INFO, float* GAP);
+JDG_API void cpjd_gep_(int* N, jdg_ccomplex* A, int* JA, int* IA, jdg_ccomplex* B, int* JB, int* IB, float* EIGS,
+                       float* RES, jdg_ccomplex* X, int* LX, int* NEIG, float* SIGMA, int* ISEARCH, int* NINIT,
+                       int* MADSPACE, int* ITER, float* TOL, float* SHIFT, float* DROPTOL, float* MEM, int* ICNTL,
+                       int* IPRINT, int* INFO, float* GAP);
+JDG_API void cpjdrevcom_(int* N, jdg_ccomplex* A, int* JA, int* IA, float* EIGS, float* RES, jdg_ccomplex* X, int* LX,
+                         int* NEIG, float* SIGMA, int* ISEARCH, int* NINIT, int* MADSPACE, int* ITER, float* TOL,
+                         float* SHIFT, float* DROPTOL, float* MEM, int* ICNTL, int* IJOB, int* NDX1, int* NDX2,
+                         int* IPRINT, int* INFO, float* GAP);
+JDG_API void cpjdrevcom_gep_(int* N, jdg_ccomplex* A, int* JA, int* IA, jdg_ccomplex* B, int* JB, int* IB,
+                             float* EIGS, float* RES, jdg_ccomplex* X, int* LX, int* NEIG, float* SIGMA, int* ISEARCH,
+                             int* NINIT, int* MADSPACE, int* ITER, float* TOL, float* SHIFT, float* DROPTOL,
+                             float* MEM, int* ICNTL, int* IJOB, int* NDX1, int* NDX2, int* NDX3, int* IPRINT,
+                             int* INFO, float* GAP);
+JDG_API void cjdrevcom_(int* N, float* EIGS, float* RES, jdg_ccomplex* X, int* LX, int* NEIG, float* SIGMA,
+                        int* ISEARCH, int* NINIT, int* MADSPACE, int* ITER, float* TOL, int* IJOB, int* NDX1,
+                        int* NDX2, int* IPRINT, int* INFO, float* GAP);
+JDG_API void cjdrevcom_gep_(int* N, float* EIGS, float* RES, jdg_ccomplex* X, int* LX, int* NEIG, float* SIGMA,
+                            int* ISEARCH, int* NINIT, int* MADSPACE, int* ITER, float* TOL, int* IJOB, int* NDX1,
+                            int* NDX2, int* NDX3, int* IPRINT, int* INFO, float* GAP);
+JDG_API void cpjdcleanup_(void);
 
 /* Number of visible CUDA devices (0 without a GPU). */
 JDG_API int jdgpu_device_count(void);

@@ -29,7 +29,7 @@ ORACLE_LIB = os.path.join(ORACLE_DIR, "_build", "liboracle.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hidden", "--expt-relaxed-constexpr",
            "-I" + os.path.join(ROOT, "include")]
-UNITS = ["kernels.cu", "devjd.cu", "driver.cu", "grad.cu"]
+UNITS = ["kernels.cu", "devjd.cu", "driver.cu", "grad.cu", "single.cpp"]
 # (source, object, extra flags) of the ILP64 library's own units
 UNITS64 = [("driver.cu", "driver_i32.o", ["-DJDG_ILP64_INNER"]), ("ilp64.cpp", "ilp64.o", [])]
 
@@ -70,10 +70,11 @@ def build_gpu(force: bool = False, verbose: bool = False) -> str:
             print(r.stderr)
         return obj
 
-    jobs = [(u, u.replace(".cu", ".o"), []) for u in UNITS] + UNITS64
+    jobs = [(u, os.path.splitext(u)[0] + ".o", []) for u in UNITS] + UNITS64
     with cf.ThreadPoolExecutor(max_workers=len(jobs)) as ex:
         objs = list(ex.map(comp, jobs))
-    common = [o for o in objs[: len(UNITS)] if not o.endswith("driver.o")]
+    # the ILP64 library has its own drivers; the single-precision ones are 32-bit only
+    common = [o for o in objs[: len(UNITS)] if not o.endswith(("driver.o", "single.o"))]
     for lib, parts in ((LIB, objs[: len(UNITS)]), (LIB64, common + objs[len(UNITS):])):
         tmp = lib + ".tmp"
         cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *parts, "-lpthread"]
