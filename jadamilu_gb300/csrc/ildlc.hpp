@@ -295,8 +295,13 @@ int ildlc_factor(int n, const int* ia, const int* ja, const T* a, double shift, 
   const int nthr = prm.threads > 0 ? prm.threads
                                    : (int)std::min<unsigned>(16, std::max(1u, std::thread::hardware_concurrency()));
   RowPool pool(n >= 20000 ? nthr : 1);
-  std::vector<std::vector<int>> tslot(pool.size());
-  for (auto& v : tslot) v.assign(n, -1);
+  // Stamped column -> position maps of the 1x1 row updates, one per thread:
+  // an entry is valid when its stamp is the current update's, so the map
+  // needs no clearing pass between rows.
+  struct PosStamp { uint32_t stamp; int pos; };
+  std::vector<std::vector<PosStamp>> tpos(pool.size());
+  for (auto& v : tpos) v.assign(n, PosStamp{0u, -1});
+  std::vector<uint32_t> tstamp(pool.size(), 0u);
   std::vector<char> inkept(n, 0);
   std::vector<int> nbr;
   std::vector<int> dlev(n, 0);  // forward level row i would get if eliminated now
@@ -699,21 +704,39 @@ int ildlc_factor(int n, const int* ia, const int* ja, const T* a, double shift, 
             remove_col(nbr[q - nkept], k);
             return;
           }
-          int* sl = tslot[tid].data();
+          // One pass over row i maps its columns (and finds column k); the
+          // updates, the appended fill and the removal of column k are those
+          // of a slot array that is set, used and cleared per row.
+          PosStamp* ps = tpos[tid].data();
+          uint32_t stamp = ++tstamp[tid];
+          if (stamp == 0) {  // the counter wrapped: clear the map once
+            for (int c = 0; c < n; ++c) ps[c] = PosStamp{0u, -1};
+            stamp = tstamp[tid] = 1;
+          }
           int i = kept[q];
           auto& row = A.rows[i];
-          for (size_t t = 0; t < row.size(); ++t) sl[row[t].col] = (int)t;
+          size_t pk = SIZE_MAX;
+          for (size_t t = 0; t < row.size(); ++t) {
+            const int c = row[t].col;
+            ps[c] = PosStamp{stamp, (int)t};
+            if (c == k && pk == SIZE_MAX) pk = t;
+          }
           T li = lk[q];
           A.diag[i] -= T(fre(li * d * fcj(li)));
           for (size_t t = 0; t < kept.size(); ++t) {
             if (t == (size_t)q) continue;
             int j = kept[t];
             T u = li * d * fcj(lk[t]);
-            if (sl[j] >= 0) row[sl[j]].val -= u;
-            else if (fab(u) * sc[i] * sc[j] > dropS) { row.push_back({j, -u}); sl[j] = (int)row.size() - 1; }
+            if (ps[j].stamp == stamp) row[ps[j].pos].val -= u;
+            else if (fab(u) * sc[i] * sc[j] > dropS) {
+              row.push_back({j, -u});
+              ps[j] = PosStamp{stamp, (int)row.size() - 1};
+            }
           }
-          for (auto& e : row) sl[e.col] = -1;
-          remove_col(i, k);
+          if (pk != SIZE_MAX) {
+            row[pk] = row.back();
+            row.pop_back();
+          }
         });
         for (int i : kept) {
           dlev[i] = std::max(dlev[i], dlev[k] + 1);
@@ -801,21 +824,28 @@ int ildlc_factor(int n, const int* ia, const int* ja, const T* a, double shift, 
         for (size_t q = 0; q < nb.size(); ++q)
           if (keepk[q] || keepj[q]) act.push_back((int)q);
         pool.run((int)act.size(), [&](int tid, int qq) {
-          int* sl = tslot[tid].data();
+          PosStamp* ps = tpos[tid].data();
+          uint32_t stamp = ++tstamp[tid];
+          if (stamp == 0) {
+            for (int c = 0; c < n; ++c) ps[c] = PosStamp{0u, -1};
+            stamp = tstamp[tid] = 1;
+          }
           const int qa = act[qq];
           int i = nb[qa];
           auto& row = A.rows[i];
-          for (size_t t = 0; t < row.size(); ++t) sl[row[t].col] = (int)t;
+          for (size_t t = 0; t < row.size(); ++t) ps[row[t].col] = PosStamp{stamp, (int)t};
           for (int ta : act) {
             int l = nb[ta];
             T c0 = fcj(lk[ta]), c1 = fcj(lj[ta]);
             T t0 = dkk * c0 + akj * c1, t1 = fcj(akj) * c0 + djj * c1;
             T u = lk[qa] * t0 + lj[qa] * t1;
             if (l == i) { A.diag[i] -= T(fre(u)); continue; }
-            if (sl[l] >= 0) row[sl[l]].val -= u;
-            else if (fab(u) * sc[i] * sc[l] > dropS) { row.push_back({l, -u}); sl[l] = (int)row.size() - 1; }
+            if (ps[l].stamp == stamp) row[ps[l].pos].val -= u;
+            else if (fab(u) * sc[i] * sc[l] > dropS) {
+              row.push_back({l, -u});
+              ps[l] = PosStamp{stamp, (int)row.size() - 1};
+            }
           }
-          for (auto& e : row) sl[e.col] = -1;
         });
         {
           int lv = std::max(dlev[k], dlev[j]) + 1;
