@@ -723,10 +723,11 @@ int ildlc_factor(int n, const int* ia, const int* ja, const T* a, double shift, 
           }
           T li = lk[q];
           A.diag[i] -= T(fre(li * d * fcj(li)));
+          const T lid = li * d;  // u = li * d * conj(l_j), evaluated left to right
           for (size_t t = 0; t < kept.size(); ++t) {
             if (t == (size_t)q) continue;
             int j = kept[t];
-            T u = li * d * fcj(lk[t]);
+            T u = lid * fcj(lk[t]);
             if (ps[j].stamp == stamp) row[ps[j].pos].val -= u;
             else if (fab(u) * sc[i] * sc[j] > dropS) {
               row.push_back({j, -u});
