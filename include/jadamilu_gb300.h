@@ -301,7 +301,10 @@ JDG_API int jdgpu_dpjd_batch(int nprob, const int* n, double* const* a, int* con
  * default: with the built-in matvec the inner CG/sQMR iteration keeps its
  * scalars on the device and synchronises once per iteration, same arithmetic;
  * 0: one synchronisation per scalar), "revcom_device" (1: reverse-
- * communication requests on device pointers, see jdgpu_revcom_device_ptr).
+ * communication requests on device pointers, see jdgpu_revcom_device_ptr),
+ * "matching" (1: the first level of the factor takes its pivot and dropping
+ * decisions in the symmetric scale of a maximum-product matching, the role of
+ * the reference's MC64 step; default 0, the level's max-norm equilibration).
  * They apply to factors computed, and solves started, after the call. */
 JDG_API void jdgpu_set_option(const char* name, double value);
 

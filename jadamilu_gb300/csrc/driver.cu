@@ -140,6 +140,7 @@ struct Options {
   int apply_graph = 0;         // jdgpu_dildl_apply through the captured graph
   int fuse_inner = 1;          // inner iterations read their scalars back once (library operators only)
   int revcom_device = 0;       // reverse-communication requests are served on the device copy of X
+  int matching = 0;            // first factor level decides with the maximum-product matching scale
 };
 static Options g_opt;
 
@@ -724,6 +725,7 @@ int pjdinit(Global<T>& g, Printer& P, int n, typename HostOf<T>::type* a, int* j
     prm.mem = MEM;
     prm.depth_weight = g_opt.depth_weight;
     prm.droptol_schur = g_opt.drop_schur;
+    prm.matching = g_opt.matching;
     prm.threads = g.factor_threads;
     double tf0 = wall();
     int ierr = ildlc_factor<H>(n, ia, ja, a, g.shift0, gep ? ib : nullptr, gep ? jb : nullptr, gep ? b : nullptr,
@@ -1947,6 +1949,7 @@ JDG_API void jdgpu_set_option(const char* name, double value) {
   else if (!std::strcmp(name, "apply_graph")) g_opt.apply_graph = (int)value;
   else if (!std::strcmp(name, "fuse_inner")) g_opt.fuse_inner = (int)value;
   else if (!std::strcmp(name, "revcom_device")) g_opt.revcom_device = (int)value;
+  else if (!std::strcmp(name, "matching")) g_opt.matching = (int)value;
   else if (!std::strcmp(name, "verbose")) g_opt.verbose = (int)value;
 }
 

@@ -34,6 +34,8 @@
 #include <thread>
 #include <vector>
 
+#include "matching.hpp"
+
 namespace jdg {
 
 using cplx = std::complex<double>;
@@ -57,6 +59,7 @@ struct IldlcParams {
   double dense_fill = 0.25;    // a level whose active rows are at least this full is eliminated densely
   int dense_min_rows = 8192;   //   if it has at least this many rows (smaller ones are quick sparse)
   double dense_max_bytes = 16e9;  //   and its dense copy fits in this many bytes
+  int matching = 0;            // 1: first level's decisions use the maximum-product matching scale
 };
 
 template <class T> struct IldlcFactor {
@@ -574,19 +577,39 @@ int ildlc_factor(int n, const int* ia, const int* ja, const T* a, double shift, 
     const int nl = (int)level_nodes.size();
     if (level >= prm.max_levels || nl <= prm.last_level_min) last = true;
     F.level_start.push_back((int)order.size());
-    // symmetric max-norm scaling of the current level (decisions only)
-    for (int i : level_nodes) {
-      double m = fab(A.diag[i]);
-      for (auto& e : A.rows[i])
-        if (state[e.col] != 1) m = std::max(m, fab(e.val));
-      sc[i] = m > 0 ? 1.0 / std::sqrt(m) : 1.0;
-    }
-    for (int sweep = 0; sweep < 2; ++sweep)
-      for (int i : level_nodes) {
-        double m = fab(A.diag[i]) * sc[i] * sc[i];
-        for (auto& e : A.rows[i]) m = std::max(m, fab(e.val) * sc[i] * sc[e.col]);
-        if (m > 0) sc[i] /= std::sqrt(m);
+    if (level == 0 && prm.matching) {
+      // first level: the symmetric scale of a maximum-product matching
+      // (decisions only, like the equilibration below)
+      std::vector<std::vector<int>> mc(n);
+      std::vector<std::vector<double>> mm(n);
+      for (int i = 0; i < n; ++i) {
+        if (fab(A.diag[i]) > 0) {
+          mc[i].push_back(i);
+          mm[i].push_back(fab(A.diag[i]));
+        }
+        for (auto& e : A.rows[i])
+          if (fab(e.val) > 0) {
+            mc[i].push_back(e.col);
+            mm[i].push_back(fab(e.val));
+          }
       }
+      const std::vector<double> ms = matching_scale(n, mc, mm);
+      for (int i = 0; i < n; ++i) sc[i] = ms[i];
+    } else {
+      // symmetric max-norm scaling of the current level (decisions only)
+      for (int i : level_nodes) {
+        double m = fab(A.diag[i]);
+        for (auto& e : A.rows[i])
+          if (state[e.col] != 1) m = std::max(m, fab(e.val));
+        sc[i] = m > 0 ? 1.0 / std::sqrt(m) : 1.0;
+      }
+      for (int sweep = 0; sweep < 2; ++sweep)
+        for (int i : level_nodes) {
+          double m = fab(A.diag[i]) * sc[i] * sc[i];
+          for (auto& e : A.rows[i]) m = std::max(m, fab(e.val) * sc[i] * sc[e.col]);
+          if (m > 0) sc[i] /= std::sqrt(m);
+        }
+    }
     std::vector<int> deferred;
     int accepted_here = 0;
     int64_t level_entries = 0;

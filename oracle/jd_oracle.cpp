@@ -31,6 +31,7 @@ namespace orc {
 // ordering weight of the triangular-solve depth (same default as the GPU library)
 static double g_depth_weight = 64.0;
 static double g_drop_schur = -1.0;  // IldlcParams::droptol_schur (negative: its default rule)
+static int g_matching = 0;          // IldlcParams::matching
 
 static double now_s() {
   using namespace std::chrono;
@@ -264,6 +265,7 @@ int pjdinit(Global<T>& g, int n, T* a, int* ja, int* ia, const T* b, const int* 
     jdg::IldlcParams prm;
     prm.depth_weight = g_depth_weight;
     prm.droptol_schur = g_drop_schur;
+    prm.matching = g_matching;
     prm.droptol = DROPTOL;
     prm.condest = condest;
     prm.mem = MEM;
@@ -642,6 +644,23 @@ void orc_zmatveca(int n, const int* ia, const int* ja, const cplx* a, const cplx
 struct OrcFactorD { jdg::IldlcFactor<double> F; };
 void orc_set_depth_weight(double w) { orc::g_depth_weight = w; }
 void orc_set_drop_schur(double v) { orc::g_drop_schur = v; }
+void orc_set_matching(int v) { orc::g_matching = v; }
+// the factor's matching scale (project code under test) for a full symmetric
+// 0-based CSR pattern; returns the number of matched rows
+int orc_matching_scale(int n, const int* rp, const int* ci, const double* av, double* scale) {
+  std::vector<std::vector<int>> cols(n);
+  std::vector<std::vector<double>> mods(n);
+  for (int i = 0; i < n; ++i)
+    for (int q = rp[i]; q < rp[i + 1]; ++q)
+      if (av[q] != 0) {
+        cols[i].push_back(ci[q]);
+        mods[i].push_back(std::fabs(av[q]));
+      }
+  int nm = 0;
+  std::vector<double> s = jdg::matching_scale(n, cols, mods, &nm);
+  for (int i = 0; i < n; ++i) scale[i] = s[i];
+  return nm;
+}
 static int g_dense_min_rows = -1;  // IldlcParams::dense_min_rows for orc_dfactor (negative: its default)
 void orc_set_dense_min_rows(int v) { g_dense_min_rows = v; }
 static int g_threads = 0;
@@ -652,6 +671,7 @@ void* orc_dfactor(int n, const int* ia, const int* ja, const double* a, double s
   jdg::IldlcParams p;
   p.depth_weight = orc::g_depth_weight;
   p.droptol_schur = orc::g_drop_schur;
+  p.matching = orc::g_matching;
   if (g_dense_min_rows >= 0) p.dense_min_rows = g_dense_min_rows;
   p.threads = g_threads;
   p.droptol = droptol;
