@@ -32,6 +32,7 @@ namespace orc {
 static double g_depth_weight = 64.0;
 static double g_drop_schur = -1.0;  // IldlcParams::droptol_schur (negative: its default rule)
 static int g_matching = 0;          // IldlcParams::matching
+static int g_dense_min_rows = -1;   // IldlcParams::dense_min_rows (negative: its default)
 
 static double now_s() {
   using namespace std::chrono;
@@ -266,6 +267,7 @@ int pjdinit(Global<T>& g, int n, T* a, int* ja, int* ia, const T* b, const int* 
     prm.depth_weight = g_depth_weight;
     prm.droptol_schur = g_drop_schur;
     prm.matching = g_matching;
+    if (g_dense_min_rows >= 0) prm.dense_min_rows = g_dense_min_rows;
     prm.droptol = DROPTOL;
     prm.condest = condest;
     prm.mem = MEM;
@@ -661,8 +663,7 @@ int orc_matching_scale(int n, const int* rp, const int* ci, const double* av, do
   for (int i = 0; i < n; ++i) scale[i] = s[i];
   return nm;
 }
-static int g_dense_min_rows = -1;  // IldlcParams::dense_min_rows for orc_dfactor (negative: its default)
-void orc_set_dense_min_rows(int v) { g_dense_min_rows = v; }
+void orc_set_dense_min_rows(int v) { orc::g_dense_min_rows = v; }
 static int g_threads = 0;
 void orc_set_threads(int t) { g_threads = t; }
 void* orc_dfactor(int n, const int* ia, const int* ja, const double* a, double shift, double droptol, double condest,
@@ -672,7 +673,7 @@ void* orc_dfactor(int n, const int* ia, const int* ja, const double* a, double s
   p.depth_weight = orc::g_depth_weight;
   p.droptol_schur = orc::g_drop_schur;
   p.matching = orc::g_matching;
-  if (g_dense_min_rows >= 0) p.dense_min_rows = g_dense_min_rows;
+  if (orc::g_dense_min_rows >= 0) p.dense_min_rows = orc::g_dense_min_rows;
   p.threads = g_threads;
   p.droptol = droptol;
   p.condest = condest;
