@@ -92,10 +92,9 @@ template <class S> struct Copies {
     *GAP = (float)gap;
   }
   // the request's input vector into the caller's X, its results back
-  void hand_out(S* X, bool gep) {
+  void hand_out(S* X) {
     if (ijob == 2) narrow(x.data() + (ndx2 - 1), X + (ndx2 - 1), n);
     else narrow(x.data() + (ndx1 - 1), X + (ndx1 - 1), n);
-    (void)gep;
   }
   void take_back(const S* X, bool gep) {
     if (ijob == 2) {
@@ -154,7 +153,7 @@ JDG_API void spjdrevcom_(int* N, float* A, int* JA, int* IA, float* EIGS, float*
   }
   c.ndx1 = *NDX1;
   c.ndx2 = *NDX2;
-  c.hand_out(X, false);
+  c.hand_out(X);
 }
 
 JDG_API void spjdrevcom_gep_(int* N, float* A, int* JA, int* IA, float* B, int* JB, int* IB, float* EIGS, float* RES,
@@ -175,7 +174,7 @@ JDG_API void spjdrevcom_gep_(int* N, float* A, int* JA, int* IA, float* B, int* 
   c.ndx1 = *NDX1;
   c.ndx2 = *NDX2;
   c.ndx3 = *NDX3;
-  c.hand_out(X, true);
+  c.hand_out(X);
 }
 
 JDG_API void sjdrevcom_(int* N, float* EIGS, float* RES, float* X, int* LX, int* NEIG, float* SIGMA, int* ISEARCH,
@@ -194,7 +193,7 @@ JDG_API void sjdrevcom_(int* N, float* EIGS, float* RES, float* X, int* LX, int*
   }
   c.ndx1 = *NDX1;
   c.ndx2 = *NDX2;
-  c.hand_out(X, false);
+  c.hand_out(X);
 }
 
 JDG_API void sjdrevcom_gep_(int* N, float* EIGS, float* RES, float* X, int* LX, int* NEIG, float* SIGMA, int* ISEARCH,
@@ -214,7 +213,7 @@ JDG_API void sjdrevcom_gep_(int* N, float* EIGS, float* RES, float* X, int* LX, 
   c.ndx1 = *NDX1;
   c.ndx2 = *NDX2;
   c.ndx3 = *NDX3;
-  c.hand_out(X, true);
+  c.hand_out(X);
 }
 
 JDG_API void spjdcleanup_(void) {
@@ -261,7 +260,7 @@ JDG_API void cpjdrevcom_(int* N, jdg_ccomplex* A, int* JA, int* IA, float* EIGS,
   }
   c.ndx1 = *NDX1;
   c.ndx2 = *NDX2;
-  c.hand_out(X, false);
+  c.hand_out(X);
 }
 
 JDG_API void cpjdrevcom_gep_(int* N, jdg_ccomplex* A, int* JA, int* IA, jdg_ccomplex* B, int* JB, int* IB,
@@ -283,7 +282,7 @@ JDG_API void cpjdrevcom_gep_(int* N, jdg_ccomplex* A, int* JA, int* IA, jdg_ccom
   c.ndx1 = *NDX1;
   c.ndx2 = *NDX2;
   c.ndx3 = *NDX3;
-  c.hand_out(X, true);
+  c.hand_out(X);
 }
 
 JDG_API void cjdrevcom_(int* N, float* EIGS, float* RES, jdg_ccomplex* X, int* LX, int* NEIG, float* SIGMA,
@@ -302,7 +301,7 @@ JDG_API void cjdrevcom_(int* N, float* EIGS, float* RES, jdg_ccomplex* X, int* L
   }
   c.ndx1 = *NDX1;
   c.ndx2 = *NDX2;
-  c.hand_out(X, false);
+  c.hand_out(X);
 }
 
 JDG_API void cjdrevcom_gep_(int* N, float* EIGS, float* RES, jdg_ccomplex* X, int* LX, int* NEIG, float* SIGMA,
@@ -322,7 +321,7 @@ JDG_API void cjdrevcom_gep_(int* N, float* EIGS, float* RES, jdg_ccomplex* X, in
   c.ndx1 = *NDX1;
   c.ndx2 = *NDX2;
   c.ndx3 = *NDX3;
-  c.hand_out(X, true);
+  c.hand_out(X);
 }
 
 JDG_API void cpjdcleanup_(void) {
