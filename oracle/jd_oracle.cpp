@@ -24,6 +24,7 @@
 #include <stdexcept>
 
 #include "../jadamilu_gb300/csrc/ildlc.hpp"
+#include "../jadamilu_gb300/csrc/tail_inverse.hpp"
 #include "jd_core.hpp"
 
 namespace orc {
@@ -647,6 +648,26 @@ struct OrcFactorD { jdg::IldlcFactor<double> F; };
 void orc_set_depth_weight(double w) { orc::g_depth_weight = w; }
 void orc_set_drop_schur(double v) { orc::g_drop_schur = v; }
 void orc_set_matching(int v) { orc::g_matching = v; }
+// The dense-block inverse tiles (project code under test): L is unit lower
+// triangular of order m given by rows rp/ci/cv (strictly lower, local
+// columns).  Writes nt*(nt+1)/2 tiles of 64x64 doubles each into tf and tb;
+// returns nt.
+int orc_tail_inverse(int m, const long* rp, const int* ci, const double* cv, int threads, double* tf, double* tb) {
+  std::vector<int64_t> p(rp, rp + m + 1);
+  std::vector<int> c(ci, ci + rp[m]);
+  std::vector<double> v(cv, cv + rp[m]);
+  std::vector<double> f, b;
+  jdg::tail_inverse<double, double>(m, p, c, v, f, b, threads, [](double x) { return x; });
+  std::copy(f.begin(), f.end(), tf);
+  std::copy(b.begin(), b.end(), tb);
+  return (m + jdg::kTile - 1) / jdg::kTile;
+}
+// cluster work items of a tile set: 4 ints per item
+int orc_cluster_items(int nt, int lower, int per_row, int* out) {
+  std::vector<int> it = jdg::make_cluster_items(nt, lower != 0, per_row);
+  std::copy(it.begin(), it.end(), out);
+  return (int)it.size() / 4;
+}
 // the factor's matching scale (project code under test) for a full symmetric
 // 0-based CSR pattern; returns the number of matched rows
 int orc_matching_scale(int n, const int* rp, const int* ci, const double* av, double* scale) {
