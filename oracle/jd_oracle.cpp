@@ -662,6 +662,25 @@ int orc_tail_inverse(int m, const long* rp, const int* ci, const double* cv, int
   std::copy(b.begin(), b.end(), tb);
   return (m + jdg::kTile - 1) / jdg::kTile;
 }
+// The small dense solvers shared by the oracle and the GPU driver
+// (csrc/small_dense.hpp), column-major J x J, for tests against LAPACK.
+int orc_heev(int cplx, int J, void* A, double* w) {
+  return cplx ? jdd::heev<std::complex<double>>(J, (std::complex<double>*)A, J, w) : jdd::heev<double>(J, (double*)A, J, w);
+}
+int orc_hegv(int cplx, int J, void* A, void* B, double* w) {
+  return cplx ? jdd::hegv<std::complex<double>>(J, (std::complex<double>*)A, J, (std::complex<double>*)B, J, w)
+              : jdd::hegv<double>(J, (double*)A, J, (double*)B, J, w);
+}
+int orc_posv(int cplx, int J, void* N, void* M) {
+  return cplx ? jdd::posv_u<std::complex<double>>(J, (std::complex<double>*)N, J, (std::complex<double>*)M, J)
+              : jdd::posv_u<double>(J, (double*)N, J, (double*)M, J);
+}
+int orc_geev(int J, const double* A, double* wr, double* V) { return jdd::geev_right<double>(J, A, J, wr, V, J); }
+void orc_householder_q(int K, int J, const double* U, double* Q) {
+  std::vector<double> q;
+  jdd::householder_q<double>(K, J, U, K, q);
+  std::copy(q.begin(), q.end(), Q);
+}
 // cluster work items of a tile set: 4 ints per item
 int orc_cluster_items(int nt, int lower, int per_row, int* out) {
   std::vector<int> it = jdg::make_cluster_items(nt, lower != 0, per_row);
