@@ -24,6 +24,7 @@
 #include "devjd.cuh"
 #include "ildlc.hpp"
 #include "tail_inverse.hpp"
+#include "block_plan.hpp"
 #include "../../include/jadamilu_gb300.h"
 
 namespace jdg {
@@ -143,68 +144,6 @@ struct Options {
   int matching = 0;            // first factor level decides with the maximum-product matching scale
 };
 static Options g_opt;
-
-// Blocks after the bulk levels.  Each group {a, b, dense} covers forward
-// levels [a, b); dense groups are solved with the explicit inverse of their
-// diagonal block, the others are single levels.  The plan minimises a model
-// of one application (both sweeps): a level costs one launch per sweep plus
-// its entries' bytes; a dense block costs three launches per sweep (external
-// entries, tile product, reduction) plus its external entries and both tile
-// sets.  Levels before the first dense block stay on the bulk level path.
-// Shallow factors keep the level path entirely (empty plan): below a saving
-// of min_saving per application, building and uploading the tiles costs
-// more than a solve gains, and substitution order keeps the rounding of the
-// sequential algorithm.
-struct BlockGroup {
-  int a, b;
-  bool dense;
-};
-static std::vector<BlockGroup> plan_dense_blocks(const std::vector<int>& fptr, const std::vector<int64_t>& ent_f,
-                                                 const std::vector<int64_t>& ent_b, size_t elem_bytes, int dense_max,
-                                                 double min_saving) {
-  const int nfl = (int)fptr.size() - 1;
-  const double t_launch = 4e-6, bw = 5.0e12;
-  const double eb = (double)elem_bytes + 4;
-  auto c_lev = [&](int l) { return (l > 0 ? 2 : 1) * t_launch + (double)(ent_f[l] + ent_b[l]) * eb / bw; };
-  std::vector<double> best(nfl + 1, 0.0);
-  std::vector<int> nxt(nfl + 1, -1);
-  for (int a = nfl - 1; a >= 0; --a) {
-    best[a] = c_lev(a) + best[a + 1];
-    if (a == 0) continue;
-    double ent = 0;
-    for (int b = a + 1; b <= nfl; ++b) {
-      const int m = fptr[b] - fptr[a];
-      if (m > dense_max) break;
-      ent += (double)(ent_f[b - 1] + ent_b[b - 1]);
-      const double nt = (m + kTile - 1) / kTile;
-      const double c = 6 * t_launch + 2.0 * nt * (nt + 1) / 2 * kTileElems * elem_bytes / bw + ent * eb / bw;
-      if (c + best[b] < best[a]) {
-        best[a] = c + best[b];
-        nxt[a] = b;
-      }
-    }
-  }
-  double all_levels = 0;
-  for (int l = 0; l < nfl; ++l) all_levels += c_lev(l);
-  std::vector<BlockGroup> g;
-  int first = -1;
-  for (int a = 1; a < nfl; ++a)
-    if (nxt[a] >= 0) {
-      first = a;
-      break;
-    }
-  if (first < 0 || all_levels - best[0] < min_saving) return g;
-  for (int a = first; a < nfl;) {
-    if (nxt[a] >= 0) {
-      g.push_back({a, nxt[a], true});
-      a = nxt[a];
-    } else {
-      g.push_back({a, a + 1, false});
-      ++a;
-    }
-  }
-  return g;
-}
 
 // device memory for the factor arrays: cudaMalloc unless the caller supplies
 // another source

@@ -25,6 +25,7 @@
 
 #include "../jadamilu_gb300/csrc/ildlc.hpp"
 #include "../jadamilu_gb300/csrc/tail_inverse.hpp"
+#include "../jadamilu_gb300/csrc/block_plan.hpp"
 #include "jd_core.hpp"
 
 namespace orc {
@@ -680,6 +681,21 @@ void orc_householder_q(int K, int J, const double* U, double* Q) {
   std::vector<double> q;
   jdd::householder_q<double>(K, J, U, K, q);
   std::copy(q.begin(), q.end(), Q);
+}
+// the dense-block plan of a forward level structure (project code under
+// test): writes 3 ints per group {first level, end level, dense}; returns
+// the number of groups
+int orc_plan_blocks(int nfl, const int* fptr, const long* ent_f, const long* ent_b, int elem_bytes, int dense_max,
+                    double min_saving, int* out) {
+  std::vector<int> fp(fptr, fptr + nfl + 1);
+  std::vector<int64_t> ef(ent_f, ent_f + nfl), eb(ent_b, ent_b + nfl);
+  std::vector<jdg::BlockGroup> g = jdg::plan_dense_blocks(fp, ef, eb, (size_t)elem_bytes, dense_max, min_saving);
+  for (size_t i = 0; i < g.size(); ++i) {
+    out[3 * i] = g[i].a;
+    out[3 * i + 1] = g[i].b;
+    out[3 * i + 2] = g[i].dense ? 1 : 0;
+  }
+  return (int)g.size();
 }
 // cluster work items of a tile set: 4 ints per item
 int orc_cluster_items(int nt, int lower, int per_row, int* out) {
