@@ -761,6 +761,25 @@ void orc_dfactor_levels(void* h, int* flev, int* ls) {
   }
   for (size_t i = 0; i < F.level_start.size(); ++i) ls[i] = F.level_start[i];
 }
+// The factor's forward and backward level schedules (project code under
+// test) and its L in CSR: sizes first (out[0..3] = nfwd levels, nbwd levels,
+// n, nnz(L)), then with non-null arrays the schedules and L's pattern.
+void orc_dfactor_schedule(void* h, long* sizes, int* fptr, int* frows, int* bptr, int* brows, long* lp, int* li) {
+  auto& F = ((OrcFactorD*)h)->F;
+  std::vector<int> fp, fr, bp, br;
+  jdg::ildlc_levels(F, fp, fr, bp, br);
+  sizes[0] = (long)fp.size() - 1;
+  sizes[1] = (long)bp.size() - 1;
+  sizes[2] = F.n;
+  sizes[3] = (long)F.li.size();
+  if (!fptr) return;
+  std::copy(fp.begin(), fp.end(), fptr);
+  std::copy(fr.begin(), fr.end(), frows);
+  std::copy(bp.begin(), bp.end(), bptr);
+  std::copy(br.begin(), br.end(), brows);
+  for (int p = 0; p <= F.n; ++p) lp[p] = (long)F.lp[p];
+  std::copy(F.li.begin(), F.li.end(), li);
+}
 void orc_dfactor_apply(void* h, int spd, int single, const double* b, double* x) {
   auto& F = ((OrcFactorD*)h)->F;
   if (single) {
