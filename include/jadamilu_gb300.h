@@ -304,7 +304,8 @@ JDG_API int jdgpu_dpjd_batch(int nprob, const int* n, double* const* a, int* con
  * communication requests on device pointers, see jdgpu_revcom_device_ptr),
  * "matching" (1: the first level of the factor takes its pivot and dropping
  * decisions in the symmetric scale of a maximum-product matching, the role of
- * the reference's MC64 step; default 0, the level's max-norm equilibration).
+ * the reference's MC64 step; 2: also pivots the matching's 2-cycles of that
+ * level as 2x2 blocks first; default 0, the level's max-norm equilibration).
  * They apply to factors computed, and solves started, after the call. */
 JDG_API void jdgpu_set_option(const char* name, double value);
 

@@ -59,7 +59,8 @@ struct IldlcParams {
   double dense_fill = 0.25;    // a level whose active rows are at least this full is eliminated densely
   int dense_min_rows = 8192;   //   if it has at least this many rows (smaller ones are quick sparse)
   double dense_max_bytes = 16e9;  //   and its dense copy fits in this many bytes
-  int matching = 0;            // 1: first level's decisions use the maximum-product matching scale
+  int matching = 0;            // 1: first level's decisions use the maximum-product matching scale;
+                               // 2: also pivot matched 2-cycles of that level as 2x2 blocks first
 };
 
 template <class T> struct IldlcFactor {
@@ -306,6 +307,7 @@ int ildlc_factor(int n, const int* ia, const int* ja, const T* a, double shift, 
   for (auto& v : tpos) v.assign(n, PosStamp{0u, -1});
   std::vector<uint32_t> tstamp(pool.size(), 0u);
   std::vector<char> inkept(n, 0);
+  std::vector<int> mate(n, -1);  // matched 2-cycle partner (first level, matching = 2)
   std::vector<int> nbr;
   std::vector<int> dlev(n, 0);  // forward level row i would get if eliminated now
   auto qkey = [&](int i) { return (int)A.rows[i].size() + (int)(prm.depth_weight * dlev[i]); };
@@ -593,8 +595,14 @@ int ildlc_factor(int n, const int* ia, const int* ja, const T* a, double shift, 
             mm[i].push_back(fab(e.val));
           }
       }
-      const std::vector<double> ms = matching_scale(n, mc, mm);
+      std::vector<int> col_of;
+      const std::vector<double> ms = matching_scale(n, mc, mm, nullptr, &col_of);
       for (int i = 0; i < n; ++i) sc[i] = ms[i];
+      if (prm.matching >= 2)  // pairs: matched 2-cycles off the diagonal
+        for (int i = 0; i < n; ++i) {
+          const int j = col_of[i];
+          mate[i] = (j >= 0 && j != i && col_of[j] == i) ? j : -1;
+        }
     } else {
       // symmetric max-norm scaling of the current level (decisions only)
       for (int i : level_nodes) {
@@ -668,7 +676,11 @@ int ildlc_factor(int n, const int* ia, const int* ja, const T* a, double shift, 
           return (int)order.size() + 1;
         }
       } else {
-        if (dks > 0 && cmax <= kappa * dks) piv = 1;
+        const int mk = level == 0 ? mate[k] : -1;
+        if (mk >= 0 && state[mk] == 0 && nu_of(mk) <= kappa) {
+          jbest = mk;  // the matching's pair as a 2x2 pivot
+          piv = 2;
+        } else if (dks > 0 && cmax <= kappa * dks) piv = 1;
         else if (jbest >= 0 && nu_of(jbest) <= kappa) piv = 2;
         else piv = 0;
       }

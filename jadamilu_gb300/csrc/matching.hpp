@@ -32,9 +32,11 @@ namespace jdg {
 
 // Full symmetric pattern: for row i, columns cols[i][*] with moduli mods[i][*]
 // (including the diagonal when it is nonzero).  Returns the symmetric scale;
-// `matched` (optional) receives the number of matched rows.
+// `matched` (optional) receives the number of matched rows and `partner`
+// (optional) the matched column of each row (-1 when unmatched).
 inline std::vector<double> matching_scale(int n, const std::vector<std::vector<int>>& cols,
-                                          const std::vector<std::vector<double>>& mods, int* matched = nullptr) {
+                                          const std::vector<std::vector<double>>& mods, int* matched = nullptr,
+                                          std::vector<int>* partner = nullptr) {
   const double inf = std::numeric_limits<double>::infinity();
   // the matrix is symmetric: column j's entries are row j's
   std::vector<double> cmax(n, 0.0);
@@ -141,6 +143,7 @@ inline std::vector<double> matching_scale(int n, const std::vector<std::vector<i
     }
   }
   if (matched) *matched = nm;
+  if (partner) *partner = col_of_row;
   return s;
 }
 
