@@ -125,7 +125,8 @@ JDG_API void zpjdcleanup_(void);
  * double precision on widened copies of the caller's arrays, with the results
  * rounded back; reverse-communication requests convert only their vectors.
  * They share the double drivers' state: an S (C) and a D (Z) reverse-
- * communication solve cannot be in flight together.  32-bit integers only. */
+ * communication solve cannot be in flight together.  The ILP64 library
+ * (jadamilu_gb300_ilp64.h) has them with 64-bit integers. */
 JDG_API void spjd_(int* N, float* A, int* JA, int* IA, float* EIGS, float* RES, float* X, int* LX, int* NEIG,
                    float* SIGMA, int* ISEARCH, int* NINIT, int* MADSPACE, int* ITER, float* TOL, float* SHIFT,
                    float* DROPTOL, float* MEM, int* ICNTL, int* IPRINT, int* INFO, float* GAP);

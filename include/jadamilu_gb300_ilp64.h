@@ -22,10 +22,12 @@
 #ifdef __cplusplus
 #include <complex>
 typedef std::complex<double> jdg64_zcomplex;
+typedef std::complex<float> jdg64_ccomplex;
 #define JDG64_API __attribute__((visibility("default")))
 extern "C" {
 #else
 typedef struct { double re, im; } jdg64_zcomplex;
+typedef struct { float re, im; } jdg64_ccomplex;
 #define JDG64_API
 #endif
 
@@ -89,6 +91,62 @@ JDG64_API void zjdrevcom_gep_(jdg_i8* N, double* EIGS, double* RES, jdg64_zcompl
                               double* TOL, jdg_i8* IJOB, jdg_i8* NDX1, jdg_i8* NDX2, jdg_i8* NDX3, jdg_i8* IPRINT,
                               jdg_i8* INFO, double* GAP);
 JDG64_API void zpjdcleanup_(void);
+
+/* Single-precision drivers (Doc/SPJD_prototypes.f:3-798, Doc/CPJD_prototypes.f:3-798) with 64-bit
+ * integers; REAL / COMPLEX values as in jadamilu_gb300.h's spjd_ ... cpjdcleanup_. */
+JDG64_API void spjd_(jdg_i8* N, float* A, jdg_i8* JA, jdg_i8* IA, float* EIGS, float* RES, float* X, jdg_i8* LX,
+                     jdg_i8* NEIG, float* SIGMA, jdg_i8* ISEARCH, jdg_i8* NINIT, jdg_i8* MADSPACE, jdg_i8* ITER,
+                     float* TOL, float* SHIFT, float* DROPTOL, float* MEM, jdg_i8* ICNTL, jdg_i8* IPRINT,
+                     jdg_i8* INFO, float* GAP);
+JDG64_API void spjd_gep_(jdg_i8* N, float* A, jdg_i8* JA, jdg_i8* IA, float* B, jdg_i8* JB, jdg_i8* IB,
+                         float* EIGS, float* RES, float* X, jdg_i8* LX, jdg_i8* NEIG, float* SIGMA,
+                         jdg_i8* ISEARCH, jdg_i8* NINIT, jdg_i8* MADSPACE, jdg_i8* ITER, float* TOL, float* SHIFT,
+                         float* DROPTOL, float* MEM, jdg_i8* ICNTL, jdg_i8* IPRINT, jdg_i8* INFO, float* GAP);
+JDG64_API void spjdrevcom_(jdg_i8* N, float* A, jdg_i8* JA, jdg_i8* IA, float* EIGS, float* RES, float* X,
+                           jdg_i8* LX, jdg_i8* NEIG, float* SIGMA, jdg_i8* ISEARCH, jdg_i8* NINIT, jdg_i8* MADSPACE,
+                           jdg_i8* ITER, float* TOL, float* SHIFT, float* DROPTOL, float* MEM, jdg_i8* ICNTL,
+                           jdg_i8* IJOB, jdg_i8* NDX1, jdg_i8* NDX2, jdg_i8* IPRINT, jdg_i8* INFO, float* GAP);
+JDG64_API void spjdrevcom_gep_(jdg_i8* N, float* A, jdg_i8* JA, jdg_i8* IA, float* B, jdg_i8* JB, jdg_i8* IB,
+                               float* EIGS, float* RES, float* X, jdg_i8* LX, jdg_i8* NEIG, float* SIGMA,
+                               jdg_i8* ISEARCH, jdg_i8* NINIT, jdg_i8* MADSPACE, jdg_i8* ITER, float* TOL,
+                               float* SHIFT, float* DROPTOL, float* MEM, jdg_i8* ICNTL, jdg_i8* IJOB, jdg_i8* NDX1,
+                               jdg_i8* NDX2, jdg_i8* NDX3, jdg_i8* IPRINT, jdg_i8* INFO, float* GAP);
+JDG64_API void sjdrevcom_(jdg_i8* N, float* EIGS, float* RES, float* X, jdg_i8* LX, jdg_i8* NEIG, float* SIGMA,
+                          jdg_i8* ISEARCH, jdg_i8* NINIT, jdg_i8* MADSPACE, jdg_i8* ITER, float* TOL, jdg_i8* IJOB,
+                          jdg_i8* NDX1, jdg_i8* NDX2, jdg_i8* IPRINT, jdg_i8* INFO, float* GAP);
+JDG64_API void sjdrevcom_gep_(jdg_i8* N, float* EIGS, float* RES, float* X, jdg_i8* LX, jdg_i8* NEIG,
+                              float* SIGMA, jdg_i8* ISEARCH, jdg_i8* NINIT, jdg_i8* MADSPACE, jdg_i8* ITER,
+                              float* TOL, jdg_i8* IJOB, jdg_i8* NDX1, jdg_i8* NDX2, jdg_i8* NDX3, jdg_i8* IPRINT,
+                              jdg_i8* INFO, float* GAP);
+JDG64_API void spjdcleanup_(void);
+
+JDG64_API void cpjd_(jdg_i8* N, jdg64_ccomplex* A, jdg_i8* JA, jdg_i8* IA, float* EIGS, float* RES,
+                     jdg64_ccomplex* X, jdg_i8* LX, jdg_i8* NEIG, float* SIGMA, jdg_i8* ISEARCH, jdg_i8* NINIT,
+                     jdg_i8* MADSPACE, jdg_i8* ITER, float* TOL, float* SHIFT, float* DROPTOL, float* MEM,
+                     jdg_i8* ICNTL, jdg_i8* IPRINT, jdg_i8* INFO, float* GAP);
+JDG64_API void cpjd_gep_(jdg_i8* N, jdg64_ccomplex* A, jdg_i8* JA, jdg_i8* IA, jdg64_ccomplex* B, jdg_i8* JB,
+                         jdg_i8* IB, float* EIGS, float* RES, jdg64_ccomplex* X, jdg_i8* LX, jdg_i8* NEIG,
+                         float* SIGMA, jdg_i8* ISEARCH, jdg_i8* NINIT, jdg_i8* MADSPACE, jdg_i8* ITER, float* TOL,
+                         float* SHIFT, float* DROPTOL, float* MEM, jdg_i8* ICNTL, jdg_i8* IPRINT, jdg_i8* INFO,
+                         float* GAP);
+JDG64_API void cpjdrevcom_(jdg_i8* N, jdg64_ccomplex* A, jdg_i8* JA, jdg_i8* IA, float* EIGS, float* RES,
+                           jdg64_ccomplex* X, jdg_i8* LX, jdg_i8* NEIG, float* SIGMA, jdg_i8* ISEARCH, jdg_i8* NINIT,
+                           jdg_i8* MADSPACE, jdg_i8* ITER, float* TOL, float* SHIFT, float* DROPTOL, float* MEM,
+                           jdg_i8* ICNTL, jdg_i8* IJOB, jdg_i8* NDX1, jdg_i8* NDX2, jdg_i8* IPRINT, jdg_i8* INFO,
+                           float* GAP);
+JDG64_API void cpjdrevcom_gep_(jdg_i8* N, jdg64_ccomplex* A, jdg_i8* JA, jdg_i8* IA, jdg64_ccomplex* B, jdg_i8* JB,
+                               jdg_i8* IB, float* EIGS, float* RES, jdg64_ccomplex* X, jdg_i8* LX, jdg_i8* NEIG,
+                               float* SIGMA, jdg_i8* ISEARCH, jdg_i8* NINIT, jdg_i8* MADSPACE, jdg_i8* ITER,
+                               float* TOL, float* SHIFT, float* DROPTOL, float* MEM, jdg_i8* ICNTL, jdg_i8* IJOB,
+                               jdg_i8* NDX1, jdg_i8* NDX2, jdg_i8* NDX3, jdg_i8* IPRINT, jdg_i8* INFO, float* GAP);
+JDG64_API void cjdrevcom_(jdg_i8* N, float* EIGS, float* RES, jdg64_ccomplex* X, jdg_i8* LX, jdg_i8* NEIG,
+                          float* SIGMA, jdg_i8* ISEARCH, jdg_i8* NINIT, jdg_i8* MADSPACE, jdg_i8* ITER, float* TOL,
+                          jdg_i8* IJOB, jdg_i8* NDX1, jdg_i8* NDX2, jdg_i8* IPRINT, jdg_i8* INFO, float* GAP);
+JDG64_API void cjdrevcom_gep_(jdg_i8* N, float* EIGS, float* RES, jdg64_ccomplex* X, jdg_i8* LX, jdg_i8* NEIG,
+                              float* SIGMA, jdg_i8* ISEARCH, jdg_i8* NINIT, jdg_i8* MADSPACE, jdg_i8* ITER,
+                              float* TOL, jdg_i8* IJOB, jdg_i8* NDX1, jdg_i8* NDX2, jdg_i8* NDX3, jdg_i8* IPRINT,
+                              jdg_i8* INFO, float* GAP);
+JDG64_API void cpjdcleanup_(void);
 
 /* Legacy PJD, PJDREVCOM, JDREVCOM, PJDCLEANUP (src/jd/PJD_compatible.f:3-106). */
 JDG64_API void pjd_(jdg_i8* N, double* A, jdg_i8* JA, jdg_i8* IA, double* EIGS, double* RES, double* X, jdg_i8* LX,

@@ -31,7 +31,8 @@ NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=h
            "-I" + os.path.join(ROOT, "include")]
 UNITS = ["kernels.cu", "devjd.cu", "driver.cu", "grad.cu", "single.cpp"]
 # (source, object, extra flags) of the ILP64 library's own units
-UNITS64 = [("driver.cu", "driver_i32.o", ["-DJDG_ILP64_INNER"]), ("ilp64.cpp", "ilp64.o", [])]
+UNITS64 = [("driver.cu", "driver_i32.o", ["-DJDG_ILP64_INNER"]), ("single.cpp", "single_i32.o", ["-DJDG_ILP64_INNER"]),
+           ("ilp64.cpp", "ilp64.o", [])]
 
 
 def _nvcc():

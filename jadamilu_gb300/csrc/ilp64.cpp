@@ -15,6 +15,7 @@
 
 using I8 = jdg_i8;
 using Z = jdg64_zcomplex;
+using CF = jdg64_ccomplex;
 
 extern "C" {
 void jdg_i32_dpjd_(int*, double*, int*, int*, double*, double*, double*, int*, int*, double*, int*, int*, int*, int*,
@@ -45,6 +46,34 @@ void jdg_i32_zjdrevcom_(int*, double*, double*, Z*, int*, int*, double*, int*, i
 void jdg_i32_zjdrevcom_gep_(int*, double*, double*, Z*, int*, int*, double*, int*, int*, int*, int*, double*, int*,
                               int*, int*, int*, int*, int*, double*);
 void jdg_i32_zpjdcleanup_(void);
+void jdg_i32_spjd_(int*, float*, int*, int*, float*, float*, float*, int*, int*, float*, int*, int*, int*, int*,
+                     float*, float*, float*, float*, int*, int*, int*, float*);
+void jdg_i32_spjd_gep_(int*, float*, int*, int*, float*, int*, int*, float*, float*, float*, int*, int*, float*, int*,
+                         int*, int*, int*, float*, float*, float*, float*, int*, int*, int*, float*);
+void jdg_i32_spjdrevcom_(int*, float*, int*, int*, float*, float*, float*, int*, int*, float*, int*, int*, int*, int*,
+                           float*, float*, float*, float*, int*, int*, int*, int*, int*, int*, float*);
+void jdg_i32_spjdrevcom_gep_(int*, float*, int*, int*, float*, int*, int*, float*, float*, float*, int*, int*, float*,
+                               int*, int*, int*, int*, float*, float*, float*, float*, int*, int*, int*, int*,
+                               int*, int*, int*, float*);
+void jdg_i32_sjdrevcom_(int*, float*, float*, float*, int*, int*, float*, int*, int*, int*, int*, float*, int*, int*,
+                          int*, int*, int*, float*);
+void jdg_i32_sjdrevcom_gep_(int*, float*, float*, float*, int*, int*, float*, int*, int*, int*, int*, float*, int*,
+                              int*, int*, int*, int*, int*, float*);
+void jdg_i32_spjdcleanup_(void);
+void jdg_i32_cpjd_(int*, CF*, int*, int*, float*, float*, CF*, int*, int*, float*, int*, int*, int*, int*,
+                     float*, float*, float*, float*, int*, int*, int*, float*);
+void jdg_i32_cpjd_gep_(int*, CF*, int*, int*, CF*, int*, int*, float*, float*, CF*, int*, int*, float*, int*,
+                         int*, int*, int*, float*, float*, float*, float*, int*, int*, int*, float*);
+void jdg_i32_cpjdrevcom_(int*, CF*, int*, int*, float*, float*, CF*, int*, int*, float*, int*, int*, int*, int*,
+                           float*, float*, float*, float*, int*, int*, int*, int*, int*, int*, float*);
+void jdg_i32_cpjdrevcom_gep_(int*, CF*, int*, int*, CF*, int*, int*, float*, float*, CF*, int*, int*, float*,
+                               int*, int*, int*, int*, float*, float*, float*, float*, int*, int*, int*, int*,
+                               int*, int*, int*, float*);
+void jdg_i32_cjdrevcom_(int*, float*, float*, CF*, int*, int*, float*, int*, int*, int*, int*, float*, int*, int*,
+                          int*, int*, int*, float*);
+void jdg_i32_cjdrevcom_gep_(int*, float*, float*, CF*, int*, int*, float*, int*, int*, int*, int*, float*, int*,
+                              int*, int*, int*, int*, int*, float*);
+void jdg_i32_cpjdcleanup_(void);
 void jdg_i32_pjd_(int*, double*, int*, int*, double*, double*, double*, int*, int*, double*, int*, int*, int*, int*,
                   double*, double*, double*, double*, int*, int*, int*, double*);
 void jdg_i32_pjdrevcom_(int*, double*, int*, int*, double*, double*, double*, int*, int*, double*, int*, int*, int*, int*,
@@ -344,6 +373,223 @@ JDG64_API void zjdrevcom_gep_(I8* N, double* EIGS, double* RES, Z* X, I8* LX, I8
   s.store(NEIG, ITER, nullptr, INFO);
 }
 JDG64_API void zpjdcleanup_(void) { jdg_i32_zpjdcleanup_(); }
+// single-precision drivers: the same narrowing around the inner REAL / COMPLEX drivers
+JDG64_API void spjd_(I8* N, float* A, I8* JA, I8* IA, float* EIGS, float* RES, float* X, I8* LX, I8* NEIG,
+                    float* SIGMA, I8* ISEARCH, I8* NINIT, I8* MADSPACE, I8* ITER, float* TOL, float* SHIFT,
+                    float* DROPTOL, float* MEM, I8* ICNTL, I8* IPRINT, I8* INFO, float* GAP) {
+  static State s;
+  if (!s.load(N, LX, NEIG, ISEARCH, NINIT, MADSPACE, ITER, ICNTL, IPRINT) || !s.a.load(*N, IA, JA)) {
+    *INFO = -1;
+    return;
+  }
+  jdg_i32_spjd_(&s.n, A, s.a.ja.data(), s.a.ia.data(), EIGS, RES, X, &s.lx, &s.neig, SIGMA, &s.isearch, &s.ninit,
+          &s.madspace, &s.iter, TOL, SHIFT, DROPTOL, MEM, s.icntl, &s.iprint, &s.info, GAP);
+  s.a.store_ja(JA);
+  s.store(NEIG, ITER, ICNTL, INFO);
+}
+JDG64_API void spjd_gep_(I8* N, float* A, I8* JA, I8* IA, float* B, I8* JB, I8* IB, float* EIGS, float* RES,
+                        float* X, I8* LX, I8* NEIG, float* SIGMA, I8* ISEARCH, I8* NINIT, I8* MADSPACE, I8* ITER,
+                        float* TOL, float* SHIFT, float* DROPTOL, float* MEM, I8* ICNTL, I8* IPRINT, I8* INFO,
+                        float* GAP) {
+  static State s;
+  if (!s.load(N, LX, NEIG, ISEARCH, NINIT, MADSPACE, ITER, ICNTL, IPRINT) || !s.a.load(*N, IA, JA) ||
+      !s.b.load(*N, IB, JB)) {
+    *INFO = -1;
+    return;
+  }
+  jdg_i32_spjd_gep_(&s.n, A, s.a.ja.data(), s.a.ia.data(), B, s.b.ja.data(), s.b.ia.data(), EIGS, RES, X, &s.lx,
+                     &s.neig, SIGMA, &s.isearch, &s.ninit, &s.madspace, &s.iter, TOL, SHIFT, DROPTOL, MEM, s.icntl,
+                     &s.iprint, &s.info, GAP);
+  s.a.store_ja(JA);
+  s.b.store_ja(JB);
+  s.store(NEIG, ITER, ICNTL, INFO);
+}
+JDG64_API void spjdrevcom_(I8* N, float* A, I8* JA, I8* IA, float* EIGS, float* RES, float* X, I8* LX,
+                          I8* NEIG, float* SIGMA, I8* ISEARCH, I8* NINIT, I8* MADSPACE, I8* ITER, float* TOL,
+                          float* SHIFT, float* DROPTOL, float* MEM, I8* ICNTL, I8* IJOB, I8* NDX1, I8* NDX2,
+                          I8* IPRINT, I8* INFO, float* GAP) {
+  static State s;
+  if (*IJOB == 0 &&
+      (!s.load(N, LX, NEIG, ISEARCH, NINIT, MADSPACE, ITER, ICNTL, IPRINT) || !s.a.load(*N, IA, JA))) {
+    *INFO = -1;
+    return;
+  }
+  s.ijob = (int)*IJOB;
+  jdg_i32_spjdrevcom_(&s.n, A, s.a.ja.data(), s.a.ia.data(), EIGS, RES, X, &s.lx, &s.neig, SIGMA, &s.isearch, &s.ninit,
+          &s.madspace, &s.iter, TOL, SHIFT, DROPTOL, MEM, s.icntl, &s.ijob, &s.ndx1, &s.ndx2, &s.iprint, &s.info,
+          GAP);
+  *IJOB = s.ijob;
+  *NDX1 = s.ndx1;
+  *NDX2 = s.ndx2;
+  s.store(NEIG, ITER, ICNTL, INFO);
+  if (s.ijob == 0) s.a.store_ja(JA);
+}
+JDG64_API void spjdrevcom_gep_(I8* N, float* A, I8* JA, I8* IA, float* B, I8* JB, I8* IB, float* EIGS,
+                              float* RES, float* X, I8* LX, I8* NEIG, float* SIGMA, I8* ISEARCH, I8* NINIT,
+                              I8* MADSPACE, I8* ITER, float* TOL, float* SHIFT, float* DROPTOL, float* MEM,
+                              I8* ICNTL, I8* IJOB, I8* NDX1, I8* NDX2, I8* NDX3, I8* IPRINT, I8* INFO, float* GAP) {
+  static State s;
+  if (*IJOB == 0 && (!s.load(N, LX, NEIG, ISEARCH, NINIT, MADSPACE, ITER, ICNTL, IPRINT) ||
+                     !s.a.load(*N, IA, JA) || !s.b.load(*N, IB, JB))) {
+    *INFO = -1;
+    return;
+  }
+  s.ijob = (int)*IJOB;
+  jdg_i32_spjdrevcom_gep_(&s.n, A, s.a.ja.data(), s.a.ia.data(), B, s.b.ja.data(), s.b.ia.data(), EIGS, RES, X,
+                           &s.lx, &s.neig, SIGMA, &s.isearch, &s.ninit, &s.madspace, &s.iter, TOL, SHIFT, DROPTOL,
+                           MEM, s.icntl, &s.ijob, &s.ndx1, &s.ndx2, &s.ndx3, &s.iprint, &s.info, GAP);
+  *IJOB = s.ijob;
+  *NDX1 = s.ndx1;
+  *NDX2 = s.ndx2;
+  *NDX3 = s.ndx3;
+  s.store(NEIG, ITER, ICNTL, INFO);
+  if (s.ijob == 0) {
+    s.a.store_ja(JA);
+    s.b.store_ja(JB);
+  }
+}
+JDG64_API void sjdrevcom_(I8* N, float* EIGS, float* RES, float* X, I8* LX, I8* NEIG, float* SIGMA,
+                         I8* ISEARCH, I8* NINIT, I8* MADSPACE, I8* ITER, float* TOL, I8* IJOB, I8* NDX1, I8* NDX2,
+                         I8* IPRINT, I8* INFO, float* GAP) {
+  static State s;
+  if (*IJOB == 0 && !s.load(N, LX, NEIG, ISEARCH, NINIT, MADSPACE, ITER, nullptr, IPRINT)) {
+    *INFO = -1;
+    return;
+  }
+  s.ijob = (int)*IJOB;
+  jdg_i32_sjdrevcom_(&s.n, EIGS, RES, X, &s.lx, &s.neig, SIGMA, &s.isearch, &s.ninit, &s.madspace, &s.iter, TOL, &s.ijob,
+          &s.ndx1, &s.ndx2, &s.iprint, &s.info, GAP);
+  *IJOB = s.ijob;
+  *NDX1 = s.ndx1;
+  *NDX2 = s.ndx2;
+  s.store(NEIG, ITER, nullptr, INFO);
+}
+JDG64_API void sjdrevcom_gep_(I8* N, float* EIGS, float* RES, float* X, I8* LX, I8* NEIG, float* SIGMA,
+                             I8* ISEARCH, I8* NINIT, I8* MADSPACE, I8* ITER, float* TOL, I8* IJOB, I8* NDX1,
+                             I8* NDX2, I8* NDX3, I8* IPRINT, I8* INFO, float* GAP) {
+  static State s;
+  if (*IJOB == 0 && !s.load(N, LX, NEIG, ISEARCH, NINIT, MADSPACE, ITER, nullptr, IPRINT)) {
+    *INFO = -1;
+    return;
+  }
+  s.ijob = (int)*IJOB;
+  jdg_i32_sjdrevcom_gep_(&s.n, EIGS, RES, X, &s.lx, &s.neig, SIGMA, &s.isearch, &s.ninit, &s.madspace, &s.iter,
+                          TOL, &s.ijob, &s.ndx1, &s.ndx2, &s.ndx3, &s.iprint, &s.info, GAP);
+  *IJOB = s.ijob;
+  *NDX1 = s.ndx1;
+  *NDX2 = s.ndx2;
+  *NDX3 = s.ndx3;
+  s.store(NEIG, ITER, nullptr, INFO);
+}
+JDG64_API void spjdcleanup_(void) { jdg_i32_spjdcleanup_(); }
+JDG64_API void cpjd_(I8* N, CF* A, I8* JA, I8* IA, float* EIGS, float* RES, CF* X, I8* LX, I8* NEIG,
+                    float* SIGMA, I8* ISEARCH, I8* NINIT, I8* MADSPACE, I8* ITER, float* TOL, float* SHIFT,
+                    float* DROPTOL, float* MEM, I8* ICNTL, I8* IPRINT, I8* INFO, float* GAP) {
+  static State s;
+  if (!s.load(N, LX, NEIG, ISEARCH, NINIT, MADSPACE, ITER, ICNTL, IPRINT) || !s.a.load(*N, IA, JA)) {
+    *INFO = -1;
+    return;
+  }
+  jdg_i32_cpjd_(&s.n, A, s.a.ja.data(), s.a.ia.data(), EIGS, RES, X, &s.lx, &s.neig, SIGMA, &s.isearch, &s.ninit,
+          &s.madspace, &s.iter, TOL, SHIFT, DROPTOL, MEM, s.icntl, &s.iprint, &s.info, GAP);
+  s.a.store_ja(JA);
+  s.store(NEIG, ITER, ICNTL, INFO);
+}
+JDG64_API void cpjd_gep_(I8* N, CF* A, I8* JA, I8* IA, CF* B, I8* JB, I8* IB, float* EIGS, float* RES,
+                        CF* X, I8* LX, I8* NEIG, float* SIGMA, I8* ISEARCH, I8* NINIT, I8* MADSPACE, I8* ITER,
+                        float* TOL, float* SHIFT, float* DROPTOL, float* MEM, I8* ICNTL, I8* IPRINT, I8* INFO,
+                        float* GAP) {
+  static State s;
+  if (!s.load(N, LX, NEIG, ISEARCH, NINIT, MADSPACE, ITER, ICNTL, IPRINT) || !s.a.load(*N, IA, JA) ||
+      !s.b.load(*N, IB, JB)) {
+    *INFO = -1;
+    return;
+  }
+  jdg_i32_cpjd_gep_(&s.n, A, s.a.ja.data(), s.a.ia.data(), B, s.b.ja.data(), s.b.ia.data(), EIGS, RES, X, &s.lx,
+                     &s.neig, SIGMA, &s.isearch, &s.ninit, &s.madspace, &s.iter, TOL, SHIFT, DROPTOL, MEM, s.icntl,
+                     &s.iprint, &s.info, GAP);
+  s.a.store_ja(JA);
+  s.b.store_ja(JB);
+  s.store(NEIG, ITER, ICNTL, INFO);
+}
+JDG64_API void cpjdrevcom_(I8* N, CF* A, I8* JA, I8* IA, float* EIGS, float* RES, CF* X, I8* LX,
+                          I8* NEIG, float* SIGMA, I8* ISEARCH, I8* NINIT, I8* MADSPACE, I8* ITER, float* TOL,
+                          float* SHIFT, float* DROPTOL, float* MEM, I8* ICNTL, I8* IJOB, I8* NDX1, I8* NDX2,
+                          I8* IPRINT, I8* INFO, float* GAP) {
+  static State s;
+  if (*IJOB == 0 &&
+      (!s.load(N, LX, NEIG, ISEARCH, NINIT, MADSPACE, ITER, ICNTL, IPRINT) || !s.a.load(*N, IA, JA))) {
+    *INFO = -1;
+    return;
+  }
+  s.ijob = (int)*IJOB;
+  jdg_i32_cpjdrevcom_(&s.n, A, s.a.ja.data(), s.a.ia.data(), EIGS, RES, X, &s.lx, &s.neig, SIGMA, &s.isearch, &s.ninit,
+          &s.madspace, &s.iter, TOL, SHIFT, DROPTOL, MEM, s.icntl, &s.ijob, &s.ndx1, &s.ndx2, &s.iprint, &s.info,
+          GAP);
+  *IJOB = s.ijob;
+  *NDX1 = s.ndx1;
+  *NDX2 = s.ndx2;
+  s.store(NEIG, ITER, ICNTL, INFO);
+  if (s.ijob == 0) s.a.store_ja(JA);
+}
+JDG64_API void cpjdrevcom_gep_(I8* N, CF* A, I8* JA, I8* IA, CF* B, I8* JB, I8* IB, float* EIGS,
+                              float* RES, CF* X, I8* LX, I8* NEIG, float* SIGMA, I8* ISEARCH, I8* NINIT,
+                              I8* MADSPACE, I8* ITER, float* TOL, float* SHIFT, float* DROPTOL, float* MEM,
+                              I8* ICNTL, I8* IJOB, I8* NDX1, I8* NDX2, I8* NDX3, I8* IPRINT, I8* INFO, float* GAP) {
+  static State s;
+  if (*IJOB == 0 && (!s.load(N, LX, NEIG, ISEARCH, NINIT, MADSPACE, ITER, ICNTL, IPRINT) ||
+                     !s.a.load(*N, IA, JA) || !s.b.load(*N, IB, JB))) {
+    *INFO = -1;
+    return;
+  }
+  s.ijob = (int)*IJOB;
+  jdg_i32_cpjdrevcom_gep_(&s.n, A, s.a.ja.data(), s.a.ia.data(), B, s.b.ja.data(), s.b.ia.data(), EIGS, RES, X,
+                           &s.lx, &s.neig, SIGMA, &s.isearch, &s.ninit, &s.madspace, &s.iter, TOL, SHIFT, DROPTOL,
+                           MEM, s.icntl, &s.ijob, &s.ndx1, &s.ndx2, &s.ndx3, &s.iprint, &s.info, GAP);
+  *IJOB = s.ijob;
+  *NDX1 = s.ndx1;
+  *NDX2 = s.ndx2;
+  *NDX3 = s.ndx3;
+  s.store(NEIG, ITER, ICNTL, INFO);
+  if (s.ijob == 0) {
+    s.a.store_ja(JA);
+    s.b.store_ja(JB);
+  }
+}
+JDG64_API void cjdrevcom_(I8* N, float* EIGS, float* RES, CF* X, I8* LX, I8* NEIG, float* SIGMA,
+                         I8* ISEARCH, I8* NINIT, I8* MADSPACE, I8* ITER, float* TOL, I8* IJOB, I8* NDX1, I8* NDX2,
+                         I8* IPRINT, I8* INFO, float* GAP) {
+  static State s;
+  if (*IJOB == 0 && !s.load(N, LX, NEIG, ISEARCH, NINIT, MADSPACE, ITER, nullptr, IPRINT)) {
+    *INFO = -1;
+    return;
+  }
+  s.ijob = (int)*IJOB;
+  jdg_i32_cjdrevcom_(&s.n, EIGS, RES, X, &s.lx, &s.neig, SIGMA, &s.isearch, &s.ninit, &s.madspace, &s.iter, TOL, &s.ijob,
+          &s.ndx1, &s.ndx2, &s.iprint, &s.info, GAP);
+  *IJOB = s.ijob;
+  *NDX1 = s.ndx1;
+  *NDX2 = s.ndx2;
+  s.store(NEIG, ITER, nullptr, INFO);
+}
+JDG64_API void cjdrevcom_gep_(I8* N, float* EIGS, float* RES, CF* X, I8* LX, I8* NEIG, float* SIGMA,
+                             I8* ISEARCH, I8* NINIT, I8* MADSPACE, I8* ITER, float* TOL, I8* IJOB, I8* NDX1,
+                             I8* NDX2, I8* NDX3, I8* IPRINT, I8* INFO, float* GAP) {
+  static State s;
+  if (*IJOB == 0 && !s.load(N, LX, NEIG, ISEARCH, NINIT, MADSPACE, ITER, nullptr, IPRINT)) {
+    *INFO = -1;
+    return;
+  }
+  s.ijob = (int)*IJOB;
+  jdg_i32_cjdrevcom_gep_(&s.n, EIGS, RES, X, &s.lx, &s.neig, SIGMA, &s.isearch, &s.ninit, &s.madspace, &s.iter,
+                          TOL, &s.ijob, &s.ndx1, &s.ndx2, &s.ndx3, &s.iprint, &s.info, GAP);
+  *IJOB = s.ijob;
+  *NDX1 = s.ndx1;
+  *NDX2 = s.ndx2;
+  *NDX3 = s.ndx3;
+  s.store(NEIG, ITER, nullptr, INFO);
+}
+JDG64_API void cpjdcleanup_(void) { jdg_i32_cpjdcleanup_(); }
 JDG64_API void pjd_(I8* N, double* A, I8* JA, I8* IA, double* EIGS, double* RES, double* X, I8* LX, I8* NEIG,
                     double* SIGMA, I8* ISEARCH, I8* NINIT, I8* MADSPACE, I8* ITER, double* TOL, double* SHIFT,
                     double* DROPTOL, double* MEM, I8* ICNTL, I8* IPRINT, I8* INFO, double* GAP) {

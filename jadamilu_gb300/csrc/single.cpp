@@ -16,12 +16,55 @@
 // (X(NDX2) and, for _GEP, X(NDX3); X(NDX1) for a preconditioner solve) are
 // widened back.  The single drivers share the state of the double ones: a
 // reverse-communication solve of SPJDREVCOM and one of DPJDREVCOM (CPJD... and
-// ZPJD...) cannot be in flight together.  These drivers are in the 32-bit
-// integer library only.
+// ZPJD...) cannot be in flight together.
 #include <complex>
 #include <vector>
 
 #include "../../include/jadamilu_gb300.h"
+
+// In the 64-bit-integer library this unit is compiled a second time
+// (JDG_ILP64_INNER): its drivers take the internal names of the 32-bit
+// ones, call the 32-bit double drivers, and ilp64.cpp puts the 64-bit
+// wrappers in front of them.
+#ifdef JDG_ILP64_INNER
+#define JDG_S(name) jdg_i32_##name
+extern "C" {
+void jdg_i32_dpjd_(int*, double*, int*, int*, double*, double*, double*, int*, int*, double*, int*, int*, int*, int*,
+                   double*, double*, double*, double*, int*, int*, int*, double*);
+void jdg_i32_dpjd_gep_(int*, double*, int*, int*, double*, int*, int*, double*, double*, double*, int*, int*, double*,
+                       int*, int*, int*, int*, double*, double*, double*, double*, int*, int*, int*, double*);
+void jdg_i32_dpjdrevcom_(int*, double*, int*, int*, double*, double*, double*, int*, int*, double*, int*, int*, int*,
+                         int*, double*, double*, double*, double*, int*, int*, int*, int*, int*, int*, double*);
+void jdg_i32_dpjdrevcom_gep_(int*, double*, int*, int*, double*, int*, int*, double*, double*, double*, int*, int*,
+                             double*, int*, int*, int*, int*, double*, double*, double*, double*, int*, int*, int*,
+                             int*, int*, int*, int*, double*);
+void jdg_i32_djdrevcom_(int*, double*, double*, double*, int*, int*, double*, int*, int*, int*, int*, double*, int*,
+                        int*, int*, int*, int*, double*);
+void jdg_i32_djdrevcom_gep_(int*, double*, double*, double*, int*, int*, double*, int*, int*, int*, int*, double*,
+                            int*, int*, int*, int*, int*, int*, double*);
+void jdg_i32_dpjdcleanup_(void);
+void jdg_i32_zpjd_(int*, jdg_zcomplex*, int*, int*, double*, double*, jdg_zcomplex*, int*, int*, double*, int*, int*,
+                   int*, int*, double*, double*, double*, double*, int*, int*, int*, double*);
+void jdg_i32_zpjd_gep_(int*, jdg_zcomplex*, int*, int*, jdg_zcomplex*, int*, int*, double*, double*, jdg_zcomplex*,
+                       int*, int*, double*, int*, int*, int*, int*, double*, double*, double*, double*, int*, int*,
+                       int*, double*);
+void jdg_i32_zpjdrevcom_(int*, jdg_zcomplex*, int*, int*, double*, double*, jdg_zcomplex*, int*, int*, double*, int*,
+                         int*, int*, int*, double*, double*, double*, double*, int*, int*, int*, int*, int*, int*,
+                         double*);
+void jdg_i32_zpjdrevcom_gep_(int*, jdg_zcomplex*, int*, int*, jdg_zcomplex*, int*, int*, double*, double*,
+                             jdg_zcomplex*, int*, int*, double*, int*, int*, int*, int*, double*, double*, double*,
+                             double*, int*, int*, int*, int*, int*, int*, int*, double*);
+void jdg_i32_zjdrevcom_(int*, double*, double*, jdg_zcomplex*, int*, int*, double*, int*, int*, int*, int*, double*,
+                        int*, int*, int*, int*, int*, double*);
+void jdg_i32_zjdrevcom_gep_(int*, double*, double*, jdg_zcomplex*, int*, int*, double*, int*, int*, int*, int*,
+                            double*, int*, int*, int*, int*, int*, int*, double*);
+void jdg_i32_zpjdcleanup_(void);
+}
+#define JDG_SAPI
+#else
+#define JDG_S(name) name
+#define JDG_SAPI JDG_API
+#endif
 
 namespace {
 
@@ -116,35 +159,35 @@ template <class S> Copies<S>& revcom_copies(int which) {
 extern "C" {
 
 // ---------------------------------------------------------------- SPJD ----
-JDG_API void spjd_(int* N, float* A, int* JA, int* IA, float* EIGS, float* RES, float* X, int* LX, int* NEIG,
+JDG_SAPI void JDG_S(spjd_)(int* N, float* A, int* JA, int* IA, float* EIGS, float* RES, float* X, int* LX, int* NEIG,
                    float* SIGMA, int* ISEARCH, int* NINIT, int* MADSPACE, int* ITER, float* TOL, float* SHIFT,
                    float* DROPTOL, float* MEM, int* ICNTL, int* IPRINT, int* INFO, float* GAP) {
   Copies<float> c;
   c.load(*N, A, IA, nullptr, nullptr, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, SHIFT, DROPTOL, MEM, GAP);
-  dpjd_(N, c.a.data(), JA, IA, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma, ISEARCH, NINIT, MADSPACE,
+  JDG_S(dpjd_)(N, c.a.data(), JA, IA, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma, ISEARCH, NINIT, MADSPACE,
         ITER, &c.tol, &c.shift, &c.droptol, &c.mem, ICNTL, IPRINT, INFO, &c.gap);
   c.store(A, nullptr, EIGS, RES, X, SHIFT, DROPTOL, MEM, GAP);
 }
 
-JDG_API void spjd_gep_(int* N, float* A, int* JA, int* IA, float* B, int* JB, int* IB, float* EIGS, float* RES,
+JDG_SAPI void JDG_S(spjd_gep_)(int* N, float* A, int* JA, int* IA, float* B, int* JB, int* IB, float* EIGS, float* RES,
                        float* X, int* LX, int* NEIG, float* SIGMA, int* ISEARCH, int* NINIT, int* MADSPACE, int* ITER,
                        float* TOL, float* SHIFT, float* DROPTOL, float* MEM, int* ICNTL, int* IPRINT, int* INFO,
                        float* GAP) {
   Copies<float> c;
   c.load(*N, A, IA, B, IB, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, SHIFT, DROPTOL, MEM, GAP);
-  dpjd_gep_(N, c.a.data(), JA, IA, c.b.data(), JB, IB, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma,
+  JDG_S(dpjd_gep_)(N, c.a.data(), JA, IA, c.b.data(), JB, IB, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma,
             ISEARCH, NINIT, MADSPACE, ITER, &c.tol, &c.shift, &c.droptol, &c.mem, ICNTL, IPRINT, INFO, &c.gap);
   c.store(A, B, EIGS, RES, X, SHIFT, DROPTOL, MEM, GAP);
 }
 
-JDG_API void spjdrevcom_(int* N, float* A, int* JA, int* IA, float* EIGS, float* RES, float* X, int* LX, int* NEIG,
+JDG_SAPI void JDG_S(spjdrevcom_)(int* N, float* A, int* JA, int* IA, float* EIGS, float* RES, float* X, int* LX, int* NEIG,
                          float* SIGMA, int* ISEARCH, int* NINIT, int* MADSPACE, int* ITER, float* TOL, float* SHIFT,
                          float* DROPTOL, float* MEM, int* ICNTL, int* IJOB, int* NDX1, int* NDX2, int* IPRINT,
                          int* INFO, float* GAP) {
   Copies<float>& c = revcom_copies<float>(0);
   if (*IJOB == 0) c.load(*N, A, IA, nullptr, nullptr, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, SHIFT, DROPTOL, MEM, GAP);
   else c.take_back(X, false);
-  dpjdrevcom_(N, c.a.data(), JA, IA, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma, ISEARCH, NINIT,
+  JDG_S(dpjdrevcom_)(N, c.a.data(), JA, IA, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma, ISEARCH, NINIT,
               MADSPACE, ITER, &c.tol, &c.shift, &c.droptol, &c.mem, ICNTL, IJOB, NDX1, NDX2, IPRINT, INFO, &c.gap);
   c.ijob = *IJOB;
   if (*IJOB == 0) {
@@ -156,14 +199,14 @@ JDG_API void spjdrevcom_(int* N, float* A, int* JA, int* IA, float* EIGS, float*
   c.hand_out(X);
 }
 
-JDG_API void spjdrevcom_gep_(int* N, float* A, int* JA, int* IA, float* B, int* JB, int* IB, float* EIGS, float* RES,
+JDG_SAPI void JDG_S(spjdrevcom_gep_)(int* N, float* A, int* JA, int* IA, float* B, int* JB, int* IB, float* EIGS, float* RES,
                              float* X, int* LX, int* NEIG, float* SIGMA, int* ISEARCH, int* NINIT, int* MADSPACE,
                              int* ITER, float* TOL, float* SHIFT, float* DROPTOL, float* MEM, int* ICNTL, int* IJOB,
                              int* NDX1, int* NDX2, int* NDX3, int* IPRINT, int* INFO, float* GAP) {
   Copies<float>& c = revcom_copies<float>(0);
   if (*IJOB == 0) c.load(*N, A, IA, B, IB, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, SHIFT, DROPTOL, MEM, GAP);
   else c.take_back(X, true);
-  dpjdrevcom_gep_(N, c.a.data(), JA, IA, c.b.data(), JB, IB, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG,
+  JDG_S(dpjdrevcom_gep_)(N, c.a.data(), JA, IA, c.b.data(), JB, IB, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG,
                   &c.sigma, ISEARCH, NINIT, MADSPACE, ITER, &c.tol, &c.shift, &c.droptol, &c.mem, ICNTL, IJOB, NDX1,
                   NDX2, NDX3, IPRINT, INFO, &c.gap);
   c.ijob = *IJOB;
@@ -177,14 +220,14 @@ JDG_API void spjdrevcom_gep_(int* N, float* A, int* JA, int* IA, float* B, int* 
   c.hand_out(X);
 }
 
-JDG_API void sjdrevcom_(int* N, float* EIGS, float* RES, float* X, int* LX, int* NEIG, float* SIGMA, int* ISEARCH,
+JDG_SAPI void JDG_S(sjdrevcom_)(int* N, float* EIGS, float* RES, float* X, int* LX, int* NEIG, float* SIGMA, int* ISEARCH,
                         int* NINIT, int* MADSPACE, int* ITER, float* TOL, int* IJOB, int* NDX1, int* NDX2, int* IPRINT,
                         int* INFO, float* GAP) {
   Copies<float>& c = revcom_copies<float>(1);
   if (*IJOB == 0)
     c.load(*N, nullptr, nullptr, nullptr, nullptr, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, nullptr, nullptr, nullptr, GAP);
   else c.take_back(X, false);
-  djdrevcom_(N, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma, ISEARCH, NINIT, MADSPACE, ITER, &c.tol,
+  JDG_S(djdrevcom_)(N, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma, ISEARCH, NINIT, MADSPACE, ITER, &c.tol,
              IJOB, NDX1, NDX2, IPRINT, INFO, &c.gap);
   c.ijob = *IJOB;
   if (*IJOB == 0) {
@@ -196,14 +239,14 @@ JDG_API void sjdrevcom_(int* N, float* EIGS, float* RES, float* X, int* LX, int*
   c.hand_out(X);
 }
 
-JDG_API void sjdrevcom_gep_(int* N, float* EIGS, float* RES, float* X, int* LX, int* NEIG, float* SIGMA, int* ISEARCH,
+JDG_SAPI void JDG_S(sjdrevcom_gep_)(int* N, float* EIGS, float* RES, float* X, int* LX, int* NEIG, float* SIGMA, int* ISEARCH,
                             int* NINIT, int* MADSPACE, int* ITER, float* TOL, int* IJOB, int* NDX1, int* NDX2,
                             int* NDX3, int* IPRINT, int* INFO, float* GAP) {
   Copies<float>& c = revcom_copies<float>(1);
   if (*IJOB == 0)
     c.load(*N, nullptr, nullptr, nullptr, nullptr, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, nullptr, nullptr, nullptr, GAP);
   else c.take_back(X, true);
-  djdrevcom_gep_(N, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma, ISEARCH, NINIT, MADSPACE, ITER,
+  JDG_S(djdrevcom_gep_)(N, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma, ISEARCH, NINIT, MADSPACE, ITER,
                  &c.tol, IJOB, NDX1, NDX2, NDX3, IPRINT, INFO, &c.gap);
   c.ijob = *IJOB;
   if (*IJOB == 0) {
@@ -216,42 +259,42 @@ JDG_API void sjdrevcom_gep_(int* N, float* EIGS, float* RES, float* X, int* LX, 
   c.hand_out(X);
 }
 
-JDG_API void spjdcleanup_(void) {
+JDG_SAPI void JDG_S(spjdcleanup_)(void) {
   revcom_copies<float>(0) = Copies<float>();
   revcom_copies<float>(1) = Copies<float>();
-  dpjdcleanup_();
+  JDG_S(dpjdcleanup_)();
 }
 
 // ---------------------------------------------------------------- CPJD ----
-JDG_API void cpjd_(int* N, jdg_ccomplex* A, int* JA, int* IA, float* EIGS, float* RES, jdg_ccomplex* X, int* LX,
+JDG_SAPI void JDG_S(cpjd_)(int* N, jdg_ccomplex* A, int* JA, int* IA, float* EIGS, float* RES, jdg_ccomplex* X, int* LX,
                    int* NEIG, float* SIGMA, int* ISEARCH, int* NINIT, int* MADSPACE, int* ITER, float* TOL,
                    float* SHIFT, float* DROPTOL, float* MEM, int* ICNTL, int* IPRINT, int* INFO, float* GAP) {
   Copies<cf> c;
   c.load(*N, A, IA, nullptr, nullptr, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, SHIFT, DROPTOL, MEM, GAP);
-  zpjd_(N, c.a.data(), JA, IA, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma, ISEARCH, NINIT, MADSPACE,
+  JDG_S(zpjd_)(N, c.a.data(), JA, IA, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma, ISEARCH, NINIT, MADSPACE,
         ITER, &c.tol, &c.shift, &c.droptol, &c.mem, ICNTL, IPRINT, INFO, &c.gap);
   c.store(A, nullptr, EIGS, RES, X, SHIFT, DROPTOL, MEM, GAP);
 }
 
-JDG_API void cpjd_gep_(int* N, jdg_ccomplex* A, int* JA, int* IA, jdg_ccomplex* B, int* JB, int* IB, float* EIGS,
+JDG_SAPI void JDG_S(cpjd_gep_)(int* N, jdg_ccomplex* A, int* JA, int* IA, jdg_ccomplex* B, int* JB, int* IB, float* EIGS,
                        float* RES, jdg_ccomplex* X, int* LX, int* NEIG, float* SIGMA, int* ISEARCH, int* NINIT,
                        int* MADSPACE, int* ITER, float* TOL, float* SHIFT, float* DROPTOL, float* MEM, int* ICNTL,
                        int* IPRINT, int* INFO, float* GAP) {
   Copies<cf> c;
   c.load(*N, A, IA, B, IB, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, SHIFT, DROPTOL, MEM, GAP);
-  zpjd_gep_(N, c.a.data(), JA, IA, c.b.data(), JB, IB, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma,
+  JDG_S(zpjd_gep_)(N, c.a.data(), JA, IA, c.b.data(), JB, IB, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma,
             ISEARCH, NINIT, MADSPACE, ITER, &c.tol, &c.shift, &c.droptol, &c.mem, ICNTL, IPRINT, INFO, &c.gap);
   c.store(A, B, EIGS, RES, X, SHIFT, DROPTOL, MEM, GAP);
 }
 
-JDG_API void cpjdrevcom_(int* N, jdg_ccomplex* A, int* JA, int* IA, float* EIGS, float* RES, jdg_ccomplex* X, int* LX,
+JDG_SAPI void JDG_S(cpjdrevcom_)(int* N, jdg_ccomplex* A, int* JA, int* IA, float* EIGS, float* RES, jdg_ccomplex* X, int* LX,
                          int* NEIG, float* SIGMA, int* ISEARCH, int* NINIT, int* MADSPACE, int* ITER, float* TOL,
                          float* SHIFT, float* DROPTOL, float* MEM, int* ICNTL, int* IJOB, int* NDX1, int* NDX2,
                          int* IPRINT, int* INFO, float* GAP) {
   Copies<cf>& c = revcom_copies<cf>(0);
   if (*IJOB == 0) c.load(*N, A, IA, nullptr, nullptr, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, SHIFT, DROPTOL, MEM, GAP);
   else c.take_back(X, false);
-  zpjdrevcom_(N, c.a.data(), JA, IA, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma, ISEARCH, NINIT,
+  JDG_S(zpjdrevcom_)(N, c.a.data(), JA, IA, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma, ISEARCH, NINIT,
               MADSPACE, ITER, &c.tol, &c.shift, &c.droptol, &c.mem, ICNTL, IJOB, NDX1, NDX2, IPRINT, INFO, &c.gap);
   c.ijob = *IJOB;
   if (*IJOB == 0) {
@@ -263,7 +306,7 @@ JDG_API void cpjdrevcom_(int* N, jdg_ccomplex* A, int* JA, int* IA, float* EIGS,
   c.hand_out(X);
 }
 
-JDG_API void cpjdrevcom_gep_(int* N, jdg_ccomplex* A, int* JA, int* IA, jdg_ccomplex* B, int* JB, int* IB,
+JDG_SAPI void JDG_S(cpjdrevcom_gep_)(int* N, jdg_ccomplex* A, int* JA, int* IA, jdg_ccomplex* B, int* JB, int* IB,
                              float* EIGS, float* RES, jdg_ccomplex* X, int* LX, int* NEIG, float* SIGMA, int* ISEARCH,
                              int* NINIT, int* MADSPACE, int* ITER, float* TOL, float* SHIFT, float* DROPTOL,
                              float* MEM, int* ICNTL, int* IJOB, int* NDX1, int* NDX2, int* NDX3, int* IPRINT,
@@ -271,7 +314,7 @@ JDG_API void cpjdrevcom_gep_(int* N, jdg_ccomplex* A, int* JA, int* IA, jdg_ccom
   Copies<cf>& c = revcom_copies<cf>(0);
   if (*IJOB == 0) c.load(*N, A, IA, B, IB, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, SHIFT, DROPTOL, MEM, GAP);
   else c.take_back(X, true);
-  zpjdrevcom_gep_(N, c.a.data(), JA, IA, c.b.data(), JB, IB, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG,
+  JDG_S(zpjdrevcom_gep_)(N, c.a.data(), JA, IA, c.b.data(), JB, IB, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG,
                   &c.sigma, ISEARCH, NINIT, MADSPACE, ITER, &c.tol, &c.shift, &c.droptol, &c.mem, ICNTL, IJOB, NDX1,
                   NDX2, NDX3, IPRINT, INFO, &c.gap);
   c.ijob = *IJOB;
@@ -285,14 +328,14 @@ JDG_API void cpjdrevcom_gep_(int* N, jdg_ccomplex* A, int* JA, int* IA, jdg_ccom
   c.hand_out(X);
 }
 
-JDG_API void cjdrevcom_(int* N, float* EIGS, float* RES, jdg_ccomplex* X, int* LX, int* NEIG, float* SIGMA,
+JDG_SAPI void JDG_S(cjdrevcom_)(int* N, float* EIGS, float* RES, jdg_ccomplex* X, int* LX, int* NEIG, float* SIGMA,
                         int* ISEARCH, int* NINIT, int* MADSPACE, int* ITER, float* TOL, int* IJOB, int* NDX1,
                         int* NDX2, int* IPRINT, int* INFO, float* GAP) {
   Copies<cf>& c = revcom_copies<cf>(1);
   if (*IJOB == 0)
     c.load(*N, nullptr, nullptr, nullptr, nullptr, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, nullptr, nullptr, nullptr, GAP);
   else c.take_back(X, false);
-  zjdrevcom_(N, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma, ISEARCH, NINIT, MADSPACE, ITER, &c.tol,
+  JDG_S(zjdrevcom_)(N, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma, ISEARCH, NINIT, MADSPACE, ITER, &c.tol,
              IJOB, NDX1, NDX2, IPRINT, INFO, &c.gap);
   c.ijob = *IJOB;
   if (*IJOB == 0) {
@@ -304,14 +347,14 @@ JDG_API void cjdrevcom_(int* N, float* EIGS, float* RES, jdg_ccomplex* X, int* L
   c.hand_out(X);
 }
 
-JDG_API void cjdrevcom_gep_(int* N, float* EIGS, float* RES, jdg_ccomplex* X, int* LX, int* NEIG, float* SIGMA,
+JDG_SAPI void JDG_S(cjdrevcom_gep_)(int* N, float* EIGS, float* RES, jdg_ccomplex* X, int* LX, int* NEIG, float* SIGMA,
                             int* ISEARCH, int* NINIT, int* MADSPACE, int* ITER, float* TOL, int* IJOB, int* NDX1,
                             int* NDX2, int* NDX3, int* IPRINT, int* INFO, float* GAP) {
   Copies<cf>& c = revcom_copies<cf>(1);
   if (*IJOB == 0)
     c.load(*N, nullptr, nullptr, nullptr, nullptr, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, nullptr, nullptr, nullptr, GAP);
   else c.take_back(X, true);
-  zjdrevcom_gep_(N, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma, ISEARCH, NINIT, MADSPACE, ITER,
+  JDG_S(zjdrevcom_gep_)(N, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma, ISEARCH, NINIT, MADSPACE, ITER,
                  &c.tol, IJOB, NDX1, NDX2, NDX3, IPRINT, INFO, &c.gap);
   c.ijob = *IJOB;
   if (*IJOB == 0) {
@@ -324,10 +367,10 @@ JDG_API void cjdrevcom_gep_(int* N, float* EIGS, float* RES, jdg_ccomplex* X, in
   c.hand_out(X);
 }
 
-JDG_API void cpjdcleanup_(void) {
+JDG_SAPI void JDG_S(cpjdcleanup_)(void) {
   revcom_copies<cf>(0) = Copies<cf>();
   revcom_copies<cf>(1) = Copies<cf>();
-  zpjdcleanup_();
+  JDG_S(zpjdcleanup_)();
 }
 
 }  // extern "C"
