@@ -1,6 +1,6 @@
 """Batched solves (jdgpu_dpjd_batch): worker threads with their own solver
 state and CUDA stream give each problem what the single-problem driver
-gives, and the eigenvalues closest to the target."""
+gives, and every returned pair is an eigenpair of its matrix."""
 import numpy as np
 import pytest
 
