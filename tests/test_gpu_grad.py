@@ -1,7 +1,9 @@
-"""Eigenvalue gradients (jdgpu_deig_grad) on the P1-FEM generalized problem
-K x = lambda M x: against the Hellmann-Feynman formula evaluated in numpy,
-and against central finite differences of the eigenvalue sum (the
-differentiation configuration's check, at a reduced grid)."""
+"""Gradients on the P1-FEM generalized problem K x = lambda M x: eigenvalue
+gradients (jdgpu_deig_grad) against the Hellmann-Feynman formula evaluated in
+numpy and against central finite differences of the eigenvalue sum (the
+differentiation configuration's check, at a reduced grid); the gradient of an
+eigenvector loss (jdgpu_deigvec_grad, adjoint MINRES on the GPU) against
+central finite differences."""
 import numpy as np
 import pytest
 
