@@ -461,14 +461,14 @@ def run_reference(args):
     if rank != 0:
         return
     if args.workload == "batch":
-        print(json.dumps({"impl": "reference", "unavailable": "the oracle arm covers the real standard workloads "
-                                                             "(anderson, laplace)"}))
+        print(json.dumps({"impl": "reference", "unavailable": "the oracle arm covers the single-problem workloads"}))
         return
     w = make_workload(args)
-    if w["kind"] != "d":
-        print(json.dumps({"impl": "reference", "unavailable": "the oracle arm covers the real standard workloads "
-                                                             "(anderson, laplace)"}))
-        return
+    extra = {}
+    if w["kind"] == "z":
+        extra["complex_"] = True
+    elif w["kind"] == "gep":
+        extra["b"] = w["B"]
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oracle_lib
     from jadamilu_gb300 import build
@@ -482,7 +482,7 @@ def run_reference(args):
     t0 = time.perf_counter()
     kw = solve_kwargs(args, 1, w)
     kw["maxit"] = 4
-    oracle_lib.dpjd(ia, ja, a, args.neig, **kw)
+    oracle_lib.dpjd(ia, ja, a, args.neig, **kw, **extra)
     factor_s = time.perf_counter() - t0
     mv = int(os.environ.get("JDG_MATVEC_PER_SOLVE", "0")) or None
     times, iters, infos = [], [], []
@@ -491,7 +491,7 @@ def run_reference(args):
         if mv:
             kw["maxit"] = max(16, mv // 10)
         t0 = time.perf_counter()
-        r = oracle_lib.dpjd(ia, ja, a, args.neig, **kw)
+        r = oracle_lib.dpjd(ia, ja, a, args.neig, **kw, **extra)
         dt = time.perf_counter() - t0
         if step >= args.warmup:
             times.append(dt * (mv / max(1, r["iter"]) if mv else 1.0))
@@ -502,12 +502,13 @@ def run_reference(args):
               f"factor {factor_s:.1f} s on {threads} threads (untimed), solve on 1 core, "
               f"MATVECs {iters}, INFO {infos}")
     metric = METRIC if w["name"] == "anderson" else f"s to {args.neig} eigpairs at resid 1e-10 ({w['name']})"
+    outer = "c128" if w["kind"] == "z" else "f64"
+    inner = {0: outer, 1: "c64" if w["kind"] == "z" else "f32", 2: "bf16"}[args.precision]
     line = {"impl": "reference", "metric": metric, "value": v, "unit": "s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64" if args.precision == 0 else ("f64 outer / f32 factor" if args.precision == 1
-                                                        else "f64 outer / bf16 factor"),
-            "data": "synthetic (seeded splitmix64 Anderson disorder)",
+            "dtype": outer if args.precision == 0 else f"{outer} outer / {inner} factor",
+            "data": "synthetic (seeded splitmix64 generators)",
             "config": {"workload": w["desc"], "factor_s": factor_s, "matvec_per_solve": int(np.median(iters))},
             "cpu_baseline": {"value": v, "unit": "s", "cores": 1, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
