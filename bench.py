@@ -461,7 +461,7 @@ def run_reference(args):
     if rank != 0:
         return
     if args.workload == "batch":
-        print(json.dumps({"impl": "reference", "unavailable": "the oracle arm covers the single-problem workloads"}))
+        run_reference_batch(args, world)
         return
     w = make_workload(args)
     extra = {}
@@ -513,6 +513,65 @@ def run_reference(args):
             "cpu_baseline": {"value": v, "unit": "s", "cores": 1, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
+
+
+def _oracle_batch_solve(job):
+    """One problem of the batch on the CPU oracle, single-threaded (pool worker)."""
+    q, m, neig, droptol, mem, precision = job
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    sys.path.insert(0, ROOT)
+    import oracle_lib
+    from jadamilu_gb300 import matrices as M
+    oracle_lib.lib().orc_set_threads(1)
+    ia, ja, a = M.anderson3d(int(m), disorder=16.5, seed=1000 + q)
+    t0 = time.perf_counter()
+    r = oracle_lib.dpjd(ia, ja, a, neig, sigma=0.0, isearch=2, madspace=20, maxit=100000, tol=1e-10,
+                        droptol=droptol, mem=mem, icntl=(0, 0, 0, 0, precision))
+    return q, time.perf_counter() - t0, r["info"], r["iter"]
+
+
+def run_reference_batch(args, world):
+    """The batch on the host cores: the CPU oracle solves (factor included,
+    one core each) a bounded sample of the batch's problems in a process
+    pool over all host cores; the step time is the sample's wall time scaled
+    by the batch's total nnz^1.75 weight over the sample's."""
+    import multiprocessing as mp
+    from jadamilu_gb300 import build
+    build.build_oracle()
+    edges = np.random.default_rng(2).integers(16, 41, size=args.batch)
+    weight = [float(7 * int(m) ** 3) ** 1.75 for m in edges]
+    stride = max(1, int(os.environ.get("JDG_BATCH_SAMPLE_STRIDE", "8")))
+    picked = [q for q in range(args.batch) if q % stride == 0]
+    cores = os.cpu_count() or 1
+    jobs = [(q, int(edges[q]), args.neig, args.droptol, args.mem, args.precision) for q in picked]
+    ctx = mp.get_context("spawn")
+    times, infos, iters = [], [], []
+    with ctx.Pool(min(cores, len(jobs))) as pool:
+        for step in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            out = pool.map(_oracle_batch_solve, jobs)
+            dt = time.perf_counter() - t0
+            if step >= args.warmup:
+                times.append(dt * sum(weight) / sum(weight[q] for q in picked))
+                infos = [o[2] for o in out]
+                iters = [o[3] for o in out]
+    v = float(np.median(times))
+    sample = (f"CPU oracle, problems {picked} of {args.batch} (every {stride}th), factor and solve on one core "
+              f"each, {min(cores, len(jobs))} processes; wall time scaled by nnz^1.75 weight to the whole batch; "
+              f"MATVECs {iters}, INFO {infos}")
+    line = {"impl": "reference",
+            "metric": f"s to {args.neig} eigpairs per problem at resid 1e-10, batch of {args.batch} Anderson problems",
+            "value": v, "unit": "s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": v * 1e3, "higher_is_better": False, "scaling": "strong", "vs_baseline": None,
+            "dtype": "f64 outer / f32 factor" if args.precision == 1 else "f64",
+            "data": "synthetic (seeded splitmix64 generators)",
+            "config": {"workload": f"{args.batch} Anderson problems, edges 16..40 (seed 2), {args.neig} eigpairs "
+                                   f"closest to 0 each, TOL 1e-10, host ILDLC per problem included",
+                       "sampled_problems": len(picked)},
+            "cpu_baseline": {"value": v, "unit": "s", "cores": min(cores, len(jobs)), "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(_finite(line)))
 
 
 def run_batch(args):
