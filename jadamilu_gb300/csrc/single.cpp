@@ -149,6 +149,17 @@ template <class S> struct Copies {
   }
 };
 
+// Host exceptions (allocation of the widened copies) must not cross the C
+// ABI: they end the call with INFO = -54330, the library's code for a failure
+// outside the algorithm.
+template <class F> void guarded(int* INFO, F&& body) {
+  try {
+    body();
+  } catch (...) {
+    if (INFO) *INFO = -54330;
+  }
+}
+
 template <class S> Copies<S>& revcom_copies(int which) {
   static Copies<S> c[2];  // 0: PJDREVCOM forms, 1: JDREVCOM forms
   return c[which];
@@ -162,101 +173,113 @@ extern "C" {
 JDG_SAPI void JDG_S(spjd_)(int* N, float* A, int* JA, int* IA, float* EIGS, float* RES, float* X, int* LX, int* NEIG,
                    float* SIGMA, int* ISEARCH, int* NINIT, int* MADSPACE, int* ITER, float* TOL, float* SHIFT,
                    float* DROPTOL, float* MEM, int* ICNTL, int* IPRINT, int* INFO, float* GAP) {
-  Copies<float> c;
-  c.load(*N, A, IA, nullptr, nullptr, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, SHIFT, DROPTOL, MEM, GAP);
-  JDG_S(dpjd_)(N, c.a.data(), JA, IA, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma, ISEARCH, NINIT, MADSPACE,
-        ITER, &c.tol, &c.shift, &c.droptol, &c.mem, ICNTL, IPRINT, INFO, &c.gap);
-  c.store(A, nullptr, EIGS, RES, X, SHIFT, DROPTOL, MEM, GAP);
+  guarded(INFO, [&] {
+    Copies<float> c;
+    c.load(*N, A, IA, nullptr, nullptr, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, SHIFT, DROPTOL, MEM, GAP);
+    JDG_S(dpjd_)(N, c.a.data(), JA, IA, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma, ISEARCH, NINIT, MADSPACE,
+          ITER, &c.tol, &c.shift, &c.droptol, &c.mem, ICNTL, IPRINT, INFO, &c.gap);
+    c.store(A, nullptr, EIGS, RES, X, SHIFT, DROPTOL, MEM, GAP);
+  });
 }
 
 JDG_SAPI void JDG_S(spjd_gep_)(int* N, float* A, int* JA, int* IA, float* B, int* JB, int* IB, float* EIGS, float* RES,
                        float* X, int* LX, int* NEIG, float* SIGMA, int* ISEARCH, int* NINIT, int* MADSPACE, int* ITER,
                        float* TOL, float* SHIFT, float* DROPTOL, float* MEM, int* ICNTL, int* IPRINT, int* INFO,
                        float* GAP) {
-  Copies<float> c;
-  c.load(*N, A, IA, B, IB, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, SHIFT, DROPTOL, MEM, GAP);
-  JDG_S(dpjd_gep_)(N, c.a.data(), JA, IA, c.b.data(), JB, IB, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma,
-            ISEARCH, NINIT, MADSPACE, ITER, &c.tol, &c.shift, &c.droptol, &c.mem, ICNTL, IPRINT, INFO, &c.gap);
-  c.store(A, B, EIGS, RES, X, SHIFT, DROPTOL, MEM, GAP);
+  guarded(INFO, [&] {
+    Copies<float> c;
+    c.load(*N, A, IA, B, IB, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, SHIFT, DROPTOL, MEM, GAP);
+    JDG_S(dpjd_gep_)(N, c.a.data(), JA, IA, c.b.data(), JB, IB, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma,
+              ISEARCH, NINIT, MADSPACE, ITER, &c.tol, &c.shift, &c.droptol, &c.mem, ICNTL, IPRINT, INFO, &c.gap);
+    c.store(A, B, EIGS, RES, X, SHIFT, DROPTOL, MEM, GAP);
+  });
 }
 
 JDG_SAPI void JDG_S(spjdrevcom_)(int* N, float* A, int* JA, int* IA, float* EIGS, float* RES, float* X, int* LX, int* NEIG,
                          float* SIGMA, int* ISEARCH, int* NINIT, int* MADSPACE, int* ITER, float* TOL, float* SHIFT,
                          float* DROPTOL, float* MEM, int* ICNTL, int* IJOB, int* NDX1, int* NDX2, int* IPRINT,
                          int* INFO, float* GAP) {
-  Copies<float>& c = revcom_copies<float>(0);
-  if (*IJOB == 0) c.load(*N, A, IA, nullptr, nullptr, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, SHIFT, DROPTOL, MEM, GAP);
-  else c.take_back(X, false);
-  JDG_S(dpjdrevcom_)(N, c.a.data(), JA, IA, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma, ISEARCH, NINIT,
-              MADSPACE, ITER, &c.tol, &c.shift, &c.droptol, &c.mem, ICNTL, IJOB, NDX1, NDX2, IPRINT, INFO, &c.gap);
-  c.ijob = *IJOB;
-  if (*IJOB == 0) {
-    c.store(A, nullptr, EIGS, RES, X, SHIFT, DROPTOL, MEM, GAP);
-    return;
-  }
-  c.ndx1 = *NDX1;
-  c.ndx2 = *NDX2;
-  c.hand_out(X);
+  guarded(INFO, [&] {
+    Copies<float>& c = revcom_copies<float>(0);
+    if (*IJOB == 0) c.load(*N, A, IA, nullptr, nullptr, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, SHIFT, DROPTOL, MEM, GAP);
+    else c.take_back(X, false);
+    JDG_S(dpjdrevcom_)(N, c.a.data(), JA, IA, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma, ISEARCH, NINIT,
+                MADSPACE, ITER, &c.tol, &c.shift, &c.droptol, &c.mem, ICNTL, IJOB, NDX1, NDX2, IPRINT, INFO, &c.gap);
+    c.ijob = *IJOB;
+    if (*IJOB == 0) {
+      c.store(A, nullptr, EIGS, RES, X, SHIFT, DROPTOL, MEM, GAP);
+      return;
+    }
+    c.ndx1 = *NDX1;
+    c.ndx2 = *NDX2;
+    c.hand_out(X);
+  });
 }
 
 JDG_SAPI void JDG_S(spjdrevcom_gep_)(int* N, float* A, int* JA, int* IA, float* B, int* JB, int* IB, float* EIGS, float* RES,
                              float* X, int* LX, int* NEIG, float* SIGMA, int* ISEARCH, int* NINIT, int* MADSPACE,
                              int* ITER, float* TOL, float* SHIFT, float* DROPTOL, float* MEM, int* ICNTL, int* IJOB,
                              int* NDX1, int* NDX2, int* NDX3, int* IPRINT, int* INFO, float* GAP) {
-  Copies<float>& c = revcom_copies<float>(0);
-  if (*IJOB == 0) c.load(*N, A, IA, B, IB, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, SHIFT, DROPTOL, MEM, GAP);
-  else c.take_back(X, true);
-  JDG_S(dpjdrevcom_gep_)(N, c.a.data(), JA, IA, c.b.data(), JB, IB, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG,
-                  &c.sigma, ISEARCH, NINIT, MADSPACE, ITER, &c.tol, &c.shift, &c.droptol, &c.mem, ICNTL, IJOB, NDX1,
-                  NDX2, NDX3, IPRINT, INFO, &c.gap);
-  c.ijob = *IJOB;
-  if (*IJOB == 0) {
-    c.store(A, B, EIGS, RES, X, SHIFT, DROPTOL, MEM, GAP);
-    return;
-  }
-  c.ndx1 = *NDX1;
-  c.ndx2 = *NDX2;
-  c.ndx3 = *NDX3;
-  c.hand_out(X);
+  guarded(INFO, [&] {
+    Copies<float>& c = revcom_copies<float>(0);
+    if (*IJOB == 0) c.load(*N, A, IA, B, IB, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, SHIFT, DROPTOL, MEM, GAP);
+    else c.take_back(X, true);
+    JDG_S(dpjdrevcom_gep_)(N, c.a.data(), JA, IA, c.b.data(), JB, IB, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG,
+                    &c.sigma, ISEARCH, NINIT, MADSPACE, ITER, &c.tol, &c.shift, &c.droptol, &c.mem, ICNTL, IJOB, NDX1,
+                    NDX2, NDX3, IPRINT, INFO, &c.gap);
+    c.ijob = *IJOB;
+    if (*IJOB == 0) {
+      c.store(A, B, EIGS, RES, X, SHIFT, DROPTOL, MEM, GAP);
+      return;
+    }
+    c.ndx1 = *NDX1;
+    c.ndx2 = *NDX2;
+    c.ndx3 = *NDX3;
+    c.hand_out(X);
+  });
 }
 
 JDG_SAPI void JDG_S(sjdrevcom_)(int* N, float* EIGS, float* RES, float* X, int* LX, int* NEIG, float* SIGMA, int* ISEARCH,
                         int* NINIT, int* MADSPACE, int* ITER, float* TOL, int* IJOB, int* NDX1, int* NDX2, int* IPRINT,
                         int* INFO, float* GAP) {
-  Copies<float>& c = revcom_copies<float>(1);
-  if (*IJOB == 0)
-    c.load(*N, nullptr, nullptr, nullptr, nullptr, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, nullptr, nullptr, nullptr, GAP);
-  else c.take_back(X, false);
-  JDG_S(djdrevcom_)(N, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma, ISEARCH, NINIT, MADSPACE, ITER, &c.tol,
-             IJOB, NDX1, NDX2, IPRINT, INFO, &c.gap);
-  c.ijob = *IJOB;
-  if (*IJOB == 0) {
-    c.store(nullptr, nullptr, EIGS, RES, X, nullptr, nullptr, nullptr, GAP);
-    return;
-  }
-  c.ndx1 = *NDX1;
-  c.ndx2 = *NDX2;
-  c.hand_out(X);
+  guarded(INFO, [&] {
+    Copies<float>& c = revcom_copies<float>(1);
+    if (*IJOB == 0)
+      c.load(*N, nullptr, nullptr, nullptr, nullptr, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, nullptr, nullptr, nullptr, GAP);
+    else c.take_back(X, false);
+    JDG_S(djdrevcom_)(N, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma, ISEARCH, NINIT, MADSPACE, ITER, &c.tol,
+               IJOB, NDX1, NDX2, IPRINT, INFO, &c.gap);
+    c.ijob = *IJOB;
+    if (*IJOB == 0) {
+      c.store(nullptr, nullptr, EIGS, RES, X, nullptr, nullptr, nullptr, GAP);
+      return;
+    }
+    c.ndx1 = *NDX1;
+    c.ndx2 = *NDX2;
+    c.hand_out(X);
+  });
 }
 
 JDG_SAPI void JDG_S(sjdrevcom_gep_)(int* N, float* EIGS, float* RES, float* X, int* LX, int* NEIG, float* SIGMA, int* ISEARCH,
                             int* NINIT, int* MADSPACE, int* ITER, float* TOL, int* IJOB, int* NDX1, int* NDX2,
                             int* NDX3, int* IPRINT, int* INFO, float* GAP) {
-  Copies<float>& c = revcom_copies<float>(1);
-  if (*IJOB == 0)
-    c.load(*N, nullptr, nullptr, nullptr, nullptr, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, nullptr, nullptr, nullptr, GAP);
-  else c.take_back(X, true);
-  JDG_S(djdrevcom_gep_)(N, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma, ISEARCH, NINIT, MADSPACE, ITER,
-                 &c.tol, IJOB, NDX1, NDX2, NDX3, IPRINT, INFO, &c.gap);
-  c.ijob = *IJOB;
-  if (*IJOB == 0) {
-    c.store(nullptr, nullptr, EIGS, RES, X, nullptr, nullptr, nullptr, GAP);
-    return;
-  }
-  c.ndx1 = *NDX1;
-  c.ndx2 = *NDX2;
-  c.ndx3 = *NDX3;
-  c.hand_out(X);
+  guarded(INFO, [&] {
+    Copies<float>& c = revcom_copies<float>(1);
+    if (*IJOB == 0)
+      c.load(*N, nullptr, nullptr, nullptr, nullptr, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, nullptr, nullptr, nullptr, GAP);
+    else c.take_back(X, true);
+    JDG_S(djdrevcom_gep_)(N, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma, ISEARCH, NINIT, MADSPACE, ITER,
+                   &c.tol, IJOB, NDX1, NDX2, NDX3, IPRINT, INFO, &c.gap);
+    c.ijob = *IJOB;
+    if (*IJOB == 0) {
+      c.store(nullptr, nullptr, EIGS, RES, X, nullptr, nullptr, nullptr, GAP);
+      return;
+    }
+    c.ndx1 = *NDX1;
+    c.ndx2 = *NDX2;
+    c.ndx3 = *NDX3;
+    c.hand_out(X);
+  });
 }
 
 JDG_SAPI void JDG_S(spjdcleanup_)(void) {
@@ -269,41 +292,47 @@ JDG_SAPI void JDG_S(spjdcleanup_)(void) {
 JDG_SAPI void JDG_S(cpjd_)(int* N, jdg_ccomplex* A, int* JA, int* IA, float* EIGS, float* RES, jdg_ccomplex* X, int* LX,
                    int* NEIG, float* SIGMA, int* ISEARCH, int* NINIT, int* MADSPACE, int* ITER, float* TOL,
                    float* SHIFT, float* DROPTOL, float* MEM, int* ICNTL, int* IPRINT, int* INFO, float* GAP) {
-  Copies<cf> c;
-  c.load(*N, A, IA, nullptr, nullptr, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, SHIFT, DROPTOL, MEM, GAP);
-  JDG_S(zpjd_)(N, c.a.data(), JA, IA, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma, ISEARCH, NINIT, MADSPACE,
-        ITER, &c.tol, &c.shift, &c.droptol, &c.mem, ICNTL, IPRINT, INFO, &c.gap);
-  c.store(A, nullptr, EIGS, RES, X, SHIFT, DROPTOL, MEM, GAP);
+  guarded(INFO, [&] {
+    Copies<cf> c;
+    c.load(*N, A, IA, nullptr, nullptr, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, SHIFT, DROPTOL, MEM, GAP);
+    JDG_S(zpjd_)(N, c.a.data(), JA, IA, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma, ISEARCH, NINIT, MADSPACE,
+          ITER, &c.tol, &c.shift, &c.droptol, &c.mem, ICNTL, IPRINT, INFO, &c.gap);
+    c.store(A, nullptr, EIGS, RES, X, SHIFT, DROPTOL, MEM, GAP);
+  });
 }
 
 JDG_SAPI void JDG_S(cpjd_gep_)(int* N, jdg_ccomplex* A, int* JA, int* IA, jdg_ccomplex* B, int* JB, int* IB, float* EIGS,
                        float* RES, jdg_ccomplex* X, int* LX, int* NEIG, float* SIGMA, int* ISEARCH, int* NINIT,
                        int* MADSPACE, int* ITER, float* TOL, float* SHIFT, float* DROPTOL, float* MEM, int* ICNTL,
                        int* IPRINT, int* INFO, float* GAP) {
-  Copies<cf> c;
-  c.load(*N, A, IA, B, IB, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, SHIFT, DROPTOL, MEM, GAP);
-  JDG_S(zpjd_gep_)(N, c.a.data(), JA, IA, c.b.data(), JB, IB, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma,
-            ISEARCH, NINIT, MADSPACE, ITER, &c.tol, &c.shift, &c.droptol, &c.mem, ICNTL, IPRINT, INFO, &c.gap);
-  c.store(A, B, EIGS, RES, X, SHIFT, DROPTOL, MEM, GAP);
+  guarded(INFO, [&] {
+    Copies<cf> c;
+    c.load(*N, A, IA, B, IB, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, SHIFT, DROPTOL, MEM, GAP);
+    JDG_S(zpjd_gep_)(N, c.a.data(), JA, IA, c.b.data(), JB, IB, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma,
+              ISEARCH, NINIT, MADSPACE, ITER, &c.tol, &c.shift, &c.droptol, &c.mem, ICNTL, IPRINT, INFO, &c.gap);
+    c.store(A, B, EIGS, RES, X, SHIFT, DROPTOL, MEM, GAP);
+  });
 }
 
 JDG_SAPI void JDG_S(cpjdrevcom_)(int* N, jdg_ccomplex* A, int* JA, int* IA, float* EIGS, float* RES, jdg_ccomplex* X, int* LX,
                          int* NEIG, float* SIGMA, int* ISEARCH, int* NINIT, int* MADSPACE, int* ITER, float* TOL,
                          float* SHIFT, float* DROPTOL, float* MEM, int* ICNTL, int* IJOB, int* NDX1, int* NDX2,
                          int* IPRINT, int* INFO, float* GAP) {
-  Copies<cf>& c = revcom_copies<cf>(0);
-  if (*IJOB == 0) c.load(*N, A, IA, nullptr, nullptr, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, SHIFT, DROPTOL, MEM, GAP);
-  else c.take_back(X, false);
-  JDG_S(zpjdrevcom_)(N, c.a.data(), JA, IA, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma, ISEARCH, NINIT,
-              MADSPACE, ITER, &c.tol, &c.shift, &c.droptol, &c.mem, ICNTL, IJOB, NDX1, NDX2, IPRINT, INFO, &c.gap);
-  c.ijob = *IJOB;
-  if (*IJOB == 0) {
-    c.store(A, nullptr, EIGS, RES, X, SHIFT, DROPTOL, MEM, GAP);
-    return;
-  }
-  c.ndx1 = *NDX1;
-  c.ndx2 = *NDX2;
-  c.hand_out(X);
+  guarded(INFO, [&] {
+    Copies<cf>& c = revcom_copies<cf>(0);
+    if (*IJOB == 0) c.load(*N, A, IA, nullptr, nullptr, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, SHIFT, DROPTOL, MEM, GAP);
+    else c.take_back(X, false);
+    JDG_S(zpjdrevcom_)(N, c.a.data(), JA, IA, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma, ISEARCH, NINIT,
+                MADSPACE, ITER, &c.tol, &c.shift, &c.droptol, &c.mem, ICNTL, IJOB, NDX1, NDX2, IPRINT, INFO, &c.gap);
+    c.ijob = *IJOB;
+    if (*IJOB == 0) {
+      c.store(A, nullptr, EIGS, RES, X, SHIFT, DROPTOL, MEM, GAP);
+      return;
+    }
+    c.ndx1 = *NDX1;
+    c.ndx2 = *NDX2;
+    c.hand_out(X);
+  });
 }
 
 JDG_SAPI void JDG_S(cpjdrevcom_gep_)(int* N, jdg_ccomplex* A, int* JA, int* IA, jdg_ccomplex* B, int* JB, int* IB,
@@ -311,60 +340,66 @@ JDG_SAPI void JDG_S(cpjdrevcom_gep_)(int* N, jdg_ccomplex* A, int* JA, int* IA, 
                              int* NINIT, int* MADSPACE, int* ITER, float* TOL, float* SHIFT, float* DROPTOL,
                              float* MEM, int* ICNTL, int* IJOB, int* NDX1, int* NDX2, int* NDX3, int* IPRINT,
                              int* INFO, float* GAP) {
-  Copies<cf>& c = revcom_copies<cf>(0);
-  if (*IJOB == 0) c.load(*N, A, IA, B, IB, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, SHIFT, DROPTOL, MEM, GAP);
-  else c.take_back(X, true);
-  JDG_S(zpjdrevcom_gep_)(N, c.a.data(), JA, IA, c.b.data(), JB, IB, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG,
-                  &c.sigma, ISEARCH, NINIT, MADSPACE, ITER, &c.tol, &c.shift, &c.droptol, &c.mem, ICNTL, IJOB, NDX1,
-                  NDX2, NDX3, IPRINT, INFO, &c.gap);
-  c.ijob = *IJOB;
-  if (*IJOB == 0) {
-    c.store(A, B, EIGS, RES, X, SHIFT, DROPTOL, MEM, GAP);
-    return;
-  }
-  c.ndx1 = *NDX1;
-  c.ndx2 = *NDX2;
-  c.ndx3 = *NDX3;
-  c.hand_out(X);
+  guarded(INFO, [&] {
+    Copies<cf>& c = revcom_copies<cf>(0);
+    if (*IJOB == 0) c.load(*N, A, IA, B, IB, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, SHIFT, DROPTOL, MEM, GAP);
+    else c.take_back(X, true);
+    JDG_S(zpjdrevcom_gep_)(N, c.a.data(), JA, IA, c.b.data(), JB, IB, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG,
+                    &c.sigma, ISEARCH, NINIT, MADSPACE, ITER, &c.tol, &c.shift, &c.droptol, &c.mem, ICNTL, IJOB, NDX1,
+                    NDX2, NDX3, IPRINT, INFO, &c.gap);
+    c.ijob = *IJOB;
+    if (*IJOB == 0) {
+      c.store(A, B, EIGS, RES, X, SHIFT, DROPTOL, MEM, GAP);
+      return;
+    }
+    c.ndx1 = *NDX1;
+    c.ndx2 = *NDX2;
+    c.ndx3 = *NDX3;
+    c.hand_out(X);
+  });
 }
 
 JDG_SAPI void JDG_S(cjdrevcom_)(int* N, float* EIGS, float* RES, jdg_ccomplex* X, int* LX, int* NEIG, float* SIGMA,
                         int* ISEARCH, int* NINIT, int* MADSPACE, int* ITER, float* TOL, int* IJOB, int* NDX1,
                         int* NDX2, int* IPRINT, int* INFO, float* GAP) {
-  Copies<cf>& c = revcom_copies<cf>(1);
-  if (*IJOB == 0)
-    c.load(*N, nullptr, nullptr, nullptr, nullptr, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, nullptr, nullptr, nullptr, GAP);
-  else c.take_back(X, false);
-  JDG_S(zjdrevcom_)(N, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma, ISEARCH, NINIT, MADSPACE, ITER, &c.tol,
-             IJOB, NDX1, NDX2, IPRINT, INFO, &c.gap);
-  c.ijob = *IJOB;
-  if (*IJOB == 0) {
-    c.store(nullptr, nullptr, EIGS, RES, X, nullptr, nullptr, nullptr, GAP);
-    return;
-  }
-  c.ndx1 = *NDX1;
-  c.ndx2 = *NDX2;
-  c.hand_out(X);
+  guarded(INFO, [&] {
+    Copies<cf>& c = revcom_copies<cf>(1);
+    if (*IJOB == 0)
+      c.load(*N, nullptr, nullptr, nullptr, nullptr, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, nullptr, nullptr, nullptr, GAP);
+    else c.take_back(X, false);
+    JDG_S(zjdrevcom_)(N, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma, ISEARCH, NINIT, MADSPACE, ITER, &c.tol,
+               IJOB, NDX1, NDX2, IPRINT, INFO, &c.gap);
+    c.ijob = *IJOB;
+    if (*IJOB == 0) {
+      c.store(nullptr, nullptr, EIGS, RES, X, nullptr, nullptr, nullptr, GAP);
+      return;
+    }
+    c.ndx1 = *NDX1;
+    c.ndx2 = *NDX2;
+    c.hand_out(X);
+  });
 }
 
 JDG_SAPI void JDG_S(cjdrevcom_gep_)(int* N, float* EIGS, float* RES, jdg_ccomplex* X, int* LX, int* NEIG, float* SIGMA,
                             int* ISEARCH, int* NINIT, int* MADSPACE, int* ITER, float* TOL, int* IJOB, int* NDX1,
                             int* NDX2, int* NDX3, int* IPRINT, int* INFO, float* GAP) {
-  Copies<cf>& c = revcom_copies<cf>(1);
-  if (*IJOB == 0)
-    c.load(*N, nullptr, nullptr, nullptr, nullptr, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, nullptr, nullptr, nullptr, GAP);
-  else c.take_back(X, true);
-  JDG_S(zjdrevcom_gep_)(N, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma, ISEARCH, NINIT, MADSPACE, ITER,
-                 &c.tol, IJOB, NDX1, NDX2, NDX3, IPRINT, INFO, &c.gap);
-  c.ijob = *IJOB;
-  if (*IJOB == 0) {
-    c.store(nullptr, nullptr, EIGS, RES, X, nullptr, nullptr, nullptr, GAP);
-    return;
-  }
-  c.ndx1 = *NDX1;
-  c.ndx2 = *NDX2;
-  c.ndx3 = *NDX3;
-  c.hand_out(X);
+  guarded(INFO, [&] {
+    Copies<cf>& c = revcom_copies<cf>(1);
+    if (*IJOB == 0)
+      c.load(*N, nullptr, nullptr, nullptr, nullptr, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, nullptr, nullptr, nullptr, GAP);
+    else c.take_back(X, true);
+    JDG_S(zjdrevcom_gep_)(N, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma, ISEARCH, NINIT, MADSPACE, ITER,
+                   &c.tol, IJOB, NDX1, NDX2, NDX3, IPRINT, INFO, &c.gap);
+    c.ijob = *IJOB;
+    if (*IJOB == 0) {
+      c.store(nullptr, nullptr, EIGS, RES, X, nullptr, nullptr, nullptr, GAP);
+      return;
+    }
+    c.ndx1 = *NDX1;
+    c.ndx2 = *NDX2;
+    c.ndx3 = *NDX3;
+    c.hand_out(X);
+  });
 }
 
 JDG_SAPI void JDG_S(cpjdcleanup_)(void) {
