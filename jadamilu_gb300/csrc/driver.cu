@@ -2136,7 +2136,11 @@ JDG_API int jdgpu_dpjd_batch(int nprob, const int* n, double* const* a, int* con
     thread_global<double>() = nullptr;
   };
   std::vector<std::thread> th;
-  for (int w = 1; w < nw; ++w) th.emplace_back(work);
+  try {
+    for (int w = 1; w < nw; ++w) th.emplace_back(work);
+  } catch (std::exception& e) {  // fewer threads than asked: the started ones and this one share the work
+    std::fprintf(stderr, "jdgpu_dpjd_batch: %s\n", e.what());
+  }
   work();
   for (auto& t : th) t.join();
   return 0;
