@@ -23,8 +23,11 @@ solve when it fits the sample budget, else a capped number of MATVECs scaled
 by the GPU solve's MATVEC count.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
-Multi-GPU runs are independent replicas (the single-matrix path does not
-shard); rank 0 prints the line.
+                       [--workload anderson|laplace|tightbinding|fem|batch]
+Multi-GPU runs of the single-matrix workloads are independent replicas (the
+path does not shard); the batch workload splits its problems over the ranks.
+Rank 0 prints the line.  ``--impl reference`` runs the CPU oracle on the same
+workload (the batch: a sampled subset in a process pool, scaled).
 """
 from __future__ import annotations
 
