@@ -282,9 +282,19 @@ def cpu_baseline_sample(J, ia, ja, a, args, gpu_iter, w=None):
     dinv, doff, ainv, aoff = (np.zeros(n) for _ in range(4))
     L.jdgpu_dfactor_export(p(n_out), p(nnz), p(sh), p(perm), p(lp), p(li), p(lx), p(blk), p(dinv), p(doff),
                            p(ainv), p(aoff))
+    cpl, nlev, nnzf = np.zeros(1, np.int32), np.zeros(1, np.int32), np.zeros(1, np.int64)
+    L.jdgpu_dfactor_export_levels.argtypes = [C.c_void_p] * 7
+    L.jdgpu_dfactor_export_levels(p(cpl), p(nlev), p(nnzf), None, None, None, None)
+    ls = np.zeros(int(nlev[0]) + 1, np.int32)
+    fp = np.zeros(n + 1, np.int64)
+    fi = np.zeros(max(1, int(nnzf[0])), np.int32)
+    fx = np.zeros(max(1, int(nnzf[0])))
+    L.jdgpu_dfactor_export_levels(p(cpl), p(nlev), p(nnzf), p(ls), p(fp), p(fi), p(fx))
     O = oracle_lib.lib()
     O.orc_dimport_factor.argtypes = [C.c_int] + [C.c_void_p] * 9 + [C.c_double]
     O.orc_dimport_factor(n, p(perm), p(lp), p(li), p(lx), p(blk), p(dinv), p(doff), p(ainv), p(aoff), float(sh[0]))
+    O.orc_dimport_levels.argtypes = [C.c_int, C.c_int] + [C.c_void_p] * 4
+    O.orc_dimport_levels(int(cpl[0]), int(nlev[0]), p(ls), p(fp), p(fi), p(fx))
     # a short capped run gives the cost per MATVEC; a complete solve follows when it fits the budget
     kw = solve_kwargs(args, -1, w)
     kw["maxit"] = 16

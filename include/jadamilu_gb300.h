@@ -225,6 +225,12 @@ JDG_API int jdgpu_dspmv_bench(int reps, double* out);
 JDG_API int jdgpu_dfactor_export(int* n_out, long long* nnz_out, double* shift_out, int* perm, long long* lp, int* li,
                                  double* lx, signed char* blk, double* dinv, double* doff, double* ainv,
                                  double* aoff);
+/* Its level structure (level_start: nlev + 1 elimination steps) and, when
+ * coupling_out is 1, the coupling blocks F of its multilevel form as CSR over
+ * elimination steps (fp: n + 1 entries, fi/fx: nnzf).  With level_start NULL
+ * only the sizes are written.  No reference counterpart (measurement only). */
+JDG_API int jdgpu_dfactor_export_levels(int* coupling_out, int* nlev_out, long long* nnzf_out, int* level_start,
+                                        long long* fp, int* fi, double* fx);
 
 /* jdgpu_dildl_apply without allocating GPU memory.  No counterpart in the
  * reference.  For callers that cannot call cudaMalloc: applications whose GPU
@@ -235,11 +241,12 @@ JDG_API int jdgpu_dfactor_export(int* n_out, long long* nnz_out, double* shift_o
  * this library (every GPU that loads it keeps those 32 MiB until the process
  * exits); problems that do not fit are rejected with -98 before any kernel
  * runs.  Nothing in the array has to start at zero: each call writes every
- * byte it later reads.  The first call on a device looks the array's address
- * up (cudaGetSymbolAddress), so make that first call before any stream
- * capture.  All calls share the one array: calls that overlap on the GPU race
- * and must not be issued.  Arguments, results and other error codes as
- * jdgpu_dildl_apply. */
+ * byte it later reads.  Every call looks the array's address up
+ * (cudaGetSymbolAddress) with the caller's device current; the first lookup
+ * on a device may load the library's device code, so make the first call on
+ * each device before any stream capture.  All calls share the one array:
+ * calls that overlap on the GPU race and must not be issued.  Arguments,
+ * results and other error codes as jdgpu_dildl_apply. */
 JDG_API int jdgpu_dildl_apply_noalloc(int n, const int* ia, const int* ja, const double* a, double shift,
                                       double droptol, double condest, int spd, int precision, int nrhs,
                                       const double* b, double* x, long* info);

@@ -118,9 +118,10 @@ template <class S> void free_factor(DevFactor<S>& F) {
   void* ps[] = {F.orig, F.lp,  F.li,  F.lx,  F.up,  F.ui,  F.ux,    F.brows, F.blk,   F.partner, F.dv,
                 F.dof,  F.av,  F.aof, F.y,   F.dfptr, F.dbptr, F.rhs_in, F.sol_out, F.tep, F.tei, F.tev,
                 F.tip,  F.tii, F.tiv, F.dtfptr, F.tbp, F.tbi, F.tbv, F.dtbptr, F.tbrows,
-                F.part, F.xb};
+                F.part, F.xb, F.perm, F.fpp, F.fpi, F.fpx, F.fhp, F.fhi, F.fhx, F.cy, F.cyb, F.ct};
   for (void* p : ps)
     if (p) cudaFree(p);
+  for (auto& L : F.lev) free_factor(L);
   for (auto& B : F.blocks) {
     void* bs[] = {B.ep, B.ei, B.ev, B.bp, B.bi, B.bv, B.tf, B.tb, B.itf, B.itb, B.irf, B.irb};
     for (void* p : bs)
@@ -142,8 +143,33 @@ struct Options {
   int fuse_inner = 1;          // inner iterations read their scalars back once (library operators only)
   int revcom_device = 0;       // reverse-communication requests are served on the device copy of X
   int matching = 0;            // first factor level decides with the maximum-product matching scale
+  // factor form (IldlcParams) from coupled_min_n rows on: coupling blocks per
+  // level, the Schur-contribution drop rule, look-ahead pivot deferral and an
+  // exact last level once a level's matrix is a third full
+  int coupling = 1;
+  int drop_rule = 1;
+  int lookahead = 1;
+  double last_droptol = 0.0;
+  double last_fill = 1.0 / 3.0;
+  int coupled_min_n = 20000;   // smaller matrices keep one global L (coupling 0, drop rule 0)
+  int factor_verbose = 0;
 };
 static Options g_opt;
+
+// the factor options of this library on top of the caller's droptol/condest/mem
+static void factor_options(IldlcParams& p, int n) {
+  p.depth_weight = g_opt.depth_weight;
+  p.droptol_schur = g_opt.drop_schur;
+  p.matching = g_opt.matching;
+  p.verbose = g_opt.factor_verbose;
+  if (n >= g_opt.coupled_min_n) {
+    p.coupling = g_opt.coupling;
+    p.drop_rule = g_opt.drop_rule;
+    p.last_droptol = g_opt.last_droptol;
+    p.last_fill = g_opt.last_fill;
+    p.lookahead = g_opt.lookahead;
+  }
+}
 
 // device memory for the factor arrays: cudaMalloc unless the caller supplies
 // another source
@@ -155,9 +181,17 @@ struct DeviceMalloc {
   }
 };
 
+template <class S, class H, class Alloc>
+void upload_coupled(const IldlcFactor<H>& F, DevFactor<S>& D, cudaStream_t st, Alloc alloc, bool graph_io);
+
 template <class S, class H, class Alloc = DeviceMalloc>
-void upload_factor(const IldlcFactor<H>& F, DevFactor<S>& D, cudaStream_t st, Alloc alloc = Alloc()) {
+void upload_factor(const IldlcFactor<H>& F, DevFactor<S>& D, cudaStream_t st, Alloc alloc = Alloc(),
+                   bool graph_io = true) {
   free_factor(D);
+  if (F.coupling == 1) {
+    upload_coupled(F, D, st, alloc, graph_io);
+    return;
+  }
   const int n = F.n;
   // forward levels over elimination steps; solve numbering s = level order
   std::vector<int> flev(n, 0);
@@ -429,11 +463,119 @@ void upload_factor(const IldlcFactor<H>& F, DevFactor<S>& D, cudaStream_t st, Al
   }
   if (max_items > 0) D.xb = (A*)alloc(sizeof(A) * max_items);
   D.y = (A*)alloc(sizeof(A) * std::max(1, n));
-  D.rhs_in = alloc(sizeof(zc) * std::max(1, n));
-  D.sol_out = alloc(sizeof(zc) * std::max(1, n));
+  if (graph_io) {  // the input and output vectors of the captured application graph
+    D.rhs_in = alloc(sizeof(zc) * std::max(1, n));
+    D.sol_out = alloc(sizeof(zc) * std::max(1, n));
+  }
   k::ildl_plan(D, lp, up, brs);
   k::ildl_plan_bwd0(D, up, brs);
   CK(cudaStreamSynchronize(st));
+  if (g_opt.verbose) {
+    int dense_b = 0;
+    for (const auto& B : D.blocks) dense_b += B.nt > 0;
+    std::fprintf(stderr,
+                 "factor upload: n %d, L %lld, forward levels %d (bulk %d), sweep kernels %zu + %zu, blocks %zu "
+                 "(%d dense, %d rows)\n",
+                 n, (long long)D.nnz_l, nfl, Lt, D.fseg.size() / 3, D.bseg.size() / 3, D.blocks.size(), dense_b,
+                 m_tail);
+  }
+}
+
+// A factor with coupling blocks: every level becomes a sub-factor (its rows in
+// elimination order, identity permutation, the level's own L and D), F and
+// F^H are stored as CSR over elimination steps, plus the work vectors of the
+// composed application (k::ildl_apply).
+template <class S, class H, class Alloc>
+void upload_coupled(const IldlcFactor<H>& F, DevFactor<S>& D, cudaStream_t st, Alloc alloc, bool graph_io) {
+  const int n = F.n;
+  const int nl = (int)F.level_start.size() - 1;
+  D.n = n;
+  D.coupled = 1;
+  D.lstart = F.level_start;
+  D.lev.resize(nl);
+  for (int l = 0; l < nl; ++l) {
+    const int a = F.level_start[l], e = F.level_start[l + 1], m = e - a;
+    IldlcFactor<H> sub;
+    sub.n = m;
+    sub.perm.resize(m);
+    for (int i = 0; i < m; ++i) sub.perm[i] = i;
+    sub.lp.assign(m + 1, 0);
+    for (int p = a; p < e; ++p) sub.lp[p - a + 1] = sub.lp[p - a] + (F.lp[p + 1] - F.lp[p]);
+    sub.li.resize(sub.lp[m]);
+    sub.lx.resize(sub.lp[m]);
+    for (int p = a; p < e; ++p)
+      for (int64_t q = F.lp[p], o = sub.lp[p - a]; q < F.lp[p + 1]; ++q, ++o) {
+        if (F.li[q] < a) throw std::runtime_error("coupled factor: an L entry crosses a level");
+        sub.li[o] = F.li[q] - a;
+        sub.lx[o] = F.lx[q];
+      }
+    sub.blk.assign(F.blk.begin() + a, F.blk.begin() + e);
+    sub.dinv.assign(F.dinv.begin() + a, F.dinv.begin() + e);
+    sub.doff.assign(F.doff.begin() + a, F.doff.begin() + e);
+    sub.ainv.assign(F.ainv.begin() + a, F.ainv.begin() + e);
+    sub.aoff.assign(F.aoff.begin() + a, F.aoff.begin() + e);
+    sub.level_start = {0, m};
+    upload_factor(sub, D.lev[l], st, alloc, false);
+    // each level below the last is solved twice per application
+    const int mult = l + 1 < nl ? 2 : 1;
+    D.nnz_l += D.lev[l].nnz_l;
+    D.sweep_entries += mult * D.lev[l].sweep_entries;
+    D.tile_bytes += mult * D.lev[l].tile_bytes;
+  }
+  // F (rows: steps of each level's pivots, one CSR over all steps) and, per
+  // level l, F_l^H over the steps after the level: rows e_l..n-1 with their
+  // entries in the level's columns, row pointers of all levels in one array
+  std::vector<S> fpx(F.fi.size());
+  for (size_t q = 0; q < F.fi.size(); ++q) fpx[q] = StoreOf<S>::f(F.fx[q]);
+  std::vector<int64_t> fhp;
+  std::vector<int> fhi(F.fi.size());
+  std::vector<S> fhx(F.fi.size());
+  D.fh_row0.assign(std::max(0, nl - 1), 0);
+  D.fp_lanes.assign(nl, 8);
+  D.fh_lanes.assign(nl, 8);
+  int64_t base = 0;  // entries of the earlier levels' blocks
+  for (int l = 0; l + 1 < nl; ++l) {
+    const int a = F.level_start[l], e = F.level_start[l + 1], m = n - e;
+    D.fh_row0[l] = (int64_t)fhp.size();
+    std::vector<int64_t> rp(m + 1, 0);
+    for (int p = a; p < e; ++p)
+      for (int64_t q = F.fp[p]; q < F.fp[p + 1]; ++q) rp[F.fi[q] - e + 1]++;
+    for (int t = 0; t < m; ++t) rp[t + 1] += rp[t];
+    std::vector<int64_t> w(rp.begin(), rp.end() - 1);
+    for (int p = a; p < e; ++p)
+      for (int64_t q = F.fp[p]; q < F.fp[p + 1]; ++q) {
+        const int64_t o = base + w[F.fi[q] - e]++;
+        fhi[o] = p;
+        fhx[o] = StoreOf<S>::f(jdd::cj(F.fx[q]));
+      }
+    for (auto& v : rp) v += base;
+    fhp.insert(fhp.end(), rp.begin(), rp.end());
+    base = rp[m];
+    D.fp_lanes[l] = k::lanes_per_row((double)(F.fp[e] - F.fp[a]) / std::max(1, e - a));
+    D.fh_lanes[l] = k::lanes_per_row((double)(rp[m] - rp[0]) / std::max(1, m));
+  }
+  if (base != (int64_t)F.fi.size()) throw std::runtime_error("coupled factor: F entries outside their levels");
+  D.nnz_f = (int64_t)F.fi.size();
+  auto up_ = [&](auto*& dst, const auto& src) {
+    using E = typename std::remove_reference<decltype(src)>::type::value_type;
+    dst = (std::remove_reference_t<decltype(dst)>)alloc(sizeof(E) * std::max<size_t>(1, src.size()));
+    if (!src.empty()) CK(cudaMemcpyAsync(dst, src.data(), sizeof(E) * src.size(), cudaMemcpyHostToDevice, st));
+  };
+  up_(D.perm, F.perm);
+  up_(D.fpp, F.fp);
+  up_(D.fpi, F.fi);
+  up_(D.fpx, fpx);
+  up_(D.fhp, fhp);
+  up_(D.fhi, fhi);
+  up_(D.fhx, fhx);
+  D.cy = alloc(sizeof(H) * std::max(1, n));
+  D.cyb = alloc(sizeof(H) * std::max(1, n));
+  D.ct = alloc(sizeof(H) * std::max(1, n));
+  if (graph_io) {
+    D.rhs_in = alloc(sizeof(zc) * std::max(1, n));
+    D.sol_out = alloc(sizeof(zc) * std::max(1, n));
+  }
+  CK(cudaStreamSynchronize(st));  // the host arrays are released next
 }
 
 template <class T> struct LowOf { using type = float; using bf = __nv_bfloat16; };
@@ -662,9 +804,7 @@ int pjdinit(Global<T>& g, Printer& P, int n, typename HostOf<T>::type* a, int* j
     prm.droptol = DROPTOL;
     prm.condest = condest;
     prm.mem = MEM;
-    prm.depth_weight = g_opt.depth_weight;
-    prm.droptol_schur = g_opt.drop_schur;
-    prm.matching = g_opt.matching;
+    factor_options(prm, n);
     prm.threads = g.factor_threads;
     double tf0 = wall();
     int ierr = ildlc_factor<H>(n, ia, ja, a, g.shift0, gep ? ib : nullptr, gep ? jb : nullptr, gep ? b : nullptr,
@@ -949,6 +1089,15 @@ void pjd_drive(int n, typename HostOf<T>::type* a, int* ja, int* ia, typename Ho
       if (ISEARCH == 1 && *SHIFT < g.diagmin) g.shift0 = *SHIFT;
       diag_first(n, ia, ja, a);
       S.timeilu = 0;
+      // a kept factor reused in another storage precision (ICNTL(5) changed
+      // between the calls): upload the host factor in that precision once
+      if (g.F.n == n) {
+        double tu = wall();
+        if (g.precision == 1 && g.Fs.n != n) upload_factor(g.F, g.Fs, g.W.st);
+        else if (g.precision == 2 && g.Fb.n != n) upload_factor(g.F, g.Fb, g.W.st);
+        else if (g.precision == 0 && g.Fd.n != n) upload_factor(g.F, g.Fd, g.W.st);
+        g.t_upload += wall() - tu;
+      }
     }
   }
   if (ierr != 0) {
@@ -1195,8 +1344,48 @@ std::function<void(long, long)> revcom_precond(Revcom& rc, typename HostOf<T>::t
 // write of the work vector per phase (gather, two sweeps, D, scatter).
 // With a dense tail the swept entries are the bulk rows' and the tail's
 // external ones, and both tile sets are read once per application.
+// rows solved through dense blocks, and the number of blocks, over all levels
+template <class S> static double dense_rows(const DevFactor<S>& F) {
+  double r = F.m_tail;
+  for (const auto& L : F.lev) r += L.m_tail;
+  return r;
+}
+template <class S> static double dense_blocks(const DevFactor<S>& F) {
+  double b = (double)F.blocks.size();
+  for (const auto& L : F.lev) b += (double)L.blocks.size();
+  return b;
+}
+// bytes of one entry of the outer (double or double complex) vectors of a factor stored as S
+template <class S> struct OuterBytes { static constexpr double v = 8; };
+template <> struct OuterBytes<zc> { static constexpr double v = 16; };
+template <> struct OuterBytes<cc> { static constexpr double v = 16; };
+template <> struct OuterBytes<bc> { static constexpr double v = 16; };
+// Algorithmic bytes of one application, as the multilevel solve defines
+// them: every stored L entry (value and column index) and row pointer read
+// once per sweep, D, the coupling blocks F and F^H once each, the
+// permutation and the vectors.  Explicit-inverse tiles are an implementation
+// choice and are not counted (precond_bytes below counts what is streamed).
+template <class S> static double precond_bytes_alg(const DevFactor<S>& F) {
+  const double n = F.n, sz = sizeof(S), sv = sizeof(typename DevFactor<S>::A);
+  if (F.coupled) {
+    double b = 0;
+    const int nl = (int)F.lev.size();
+    for (int l = 0; l < nl; ++l) b += (l + 1 < nl ? 2.0 : 1.0) * precond_bytes_alg(F.lev[l]);
+    return b + 2.0 * (double)F.nnz_f * (sz + 4) + 2.0 * (n + 1) * 8 + n * 4 * 2 + 10.0 * n * OuterBytes<S>::v;
+  }
+  return 2.0 * (double)F.nnz_l * (sz + 4) + 2.0 * (n + 1) * 8 + n * (1 + 2 * sz) + n * 4 * 2 +
+         2.0 * n * OuterBytes<S>::v + 4.0 * n * sv;
+}
 template <class S> static double precond_bytes(const DevFactor<S>& F) {
   const double n = F.n, sz = sizeof(S), sv = sizeof(typename DevFactor<S>::A);
+  if (F.coupled) {
+    // levels below the last are solved twice; F and F^H once each; the outer
+    // vectors (8 or 16 bytes) gathered, kept, combined and scattered
+    double b = 0;
+    const int nl = (int)F.lev.size();
+    for (int l = 0; l < nl; ++l) b += (l + 1 < nl ? 2.0 : 1.0) * precond_bytes(F.lev[l]);
+    return b + 2.0 * (double)F.nnz_f * (sz + 4) + 2.0 * (n + 1) * 8 + n * 4 * 2 + 10.0 * n * OuterBytes<S>::v;
+  }
   return (double)F.sweep_entries * (sz + 4) + 2.0 * (n + 1) * 8 + 3.0 * n * 4 + n * (1 + 4 + 2 * sz) +
          2.0 * n * 8 + 8.0 * n * sv + F.tile_bytes;
 }
@@ -1209,24 +1398,17 @@ constexpr size_t kNoallocScratchBytes = size_t(32) << 20;  // 32 MiB
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];
 
 // Host code cannot use g_noalloc_scratch as a pointer (it names the host-side
-// stand-in); the device address is looked up once per device, with that
-// device current.
+// stand-in).  The device address is looked up on every call, with the
+// caller's device current: the lookup is cheap, and a cached address would
+// go stale when the context is torn down and the module loaded again (for
+// example after cudaDeviceReset).
 static void* noalloc_scratch_ptr() {
-  static std::mutex mu;
-  static void* ptrs[64] = {nullptr};
-  int dev = 0;
-  CK(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= 64) throw std::runtime_error("device index out of range");
-  std::lock_guard<std::mutex> lk(mu);
-  if (!ptrs[dev]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p)
-      throw std::runtime_error(std::string("cudaGetSymbolAddress of the scratch array failed: ") +
-                               cudaGetErrorString(e));
-    ptrs[dev] = p;
-  }
-  return ptrs[dev];
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || !p)
+    throw std::runtime_error(std::string("cudaGetSymbolAddress of the scratch array failed: ") +
+                             cudaGetErrorString(e));
+  return p;
 }
 
 struct ScratchFull : std::runtime_error {
@@ -1543,8 +1725,7 @@ JDG_API int jdgpu_dildl_apply(int n, const int* ia, const int* ja, const double*
     p.droptol = droptol;
     p.condest = condest;
     p.mem = 0;
-    p.depth_weight = g_opt.depth_weight;
-    p.droptol_schur = g_opt.drop_schur;
+    factor_options(p, n);
     IldlcFactor<double> F;
     int ierr = ildlc_factor<double>(n, ia, ja, a, shift, nullptr, nullptr, nullptr, p, F);
     if (ierr) return ierr;
@@ -1610,8 +1791,7 @@ JDG_API int jdgpu_dildl_bench(int n, const int* ia, const int* ja, const double*
     p.droptol = droptol;
     p.condest = condest;
     p.mem = 0;
-    p.depth_weight = g_opt.depth_weight;
-    p.droptol_schur = g_opt.drop_schur;
+    factor_options(p, n);
     IldlcFactor<double> F;
     double t0 = wall();
     int ierr = ildlc_factor<double>(n, ia, ja, a, shift, nullptr, nullptr, nullptr, p, F);
@@ -1660,7 +1840,7 @@ JDG_API int jdgpu_dildl_bench(int n, const int* ia, const int* ja, const double*
       out[3] = (double)bp.size() - 1;
     }
     out[4] = (double)launches;
-    out[6] = precision == 1 ? Fs.m_tail : precision == 2 ? Fb.m_tail : Fd.m_tail;
+    out[6] = precision == 1 ? dense_rows(Fs) : precision == 2 ? dense_rows(Fb) : dense_rows(Fd);
     out[5] = tf;
     out[7] = tu;
     cudaEventDestroy(e0);
@@ -1743,9 +1923,16 @@ JDG_API int jdgpu_dprecond_bench(int reps, double* out) {
     float ms = 0;
     CK(cudaEventElapsedTime(&ms, e0, e1));
     out[0] = ms / reps;
-    if (g.precision == 1) { out[1] = precond_bytes(g.Fs); out[2] = g.Fs.nnz_l; out[3] = g.Fs.m_tail; out[4] = (double)g.Fs.graph_kernels[0]; }
-    else if (g.precision == 2) { out[1] = precond_bytes(g.Fb); out[2] = g.Fb.nnz_l; out[3] = g.Fb.m_tail; out[4] = (double)g.Fb.graph_kernels[0]; }
-    else { out[1] = precond_bytes(g.Fd); out[2] = g.Fd.nnz_l; out[3] = g.Fd.m_tail; out[4] = (double)g.Fd.graph_kernels[0]; }
+    auto fill_out = [&](const auto& D) {
+      out[1] = precond_bytes(D);
+      out[2] = (double)D.nnz_l;
+      out[3] = dense_rows(D);
+      out[4] = (double)D.graph_kernels[0];
+      out[5] = precond_bytes_alg(D);
+    };
+    if (g.precision == 1) fill_out(g.Fs);
+    else if (g.precision == 2) fill_out(g.Fb);
+    else fill_out(g.Fd);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     cudaFree(b);
@@ -1817,6 +2004,23 @@ JDG_API int jdgpu_dfactor_export(int* n_out, long long* nnz_out, double* shift_o
   return 0;
 }
 
+// The level structure and coupling blocks of that factor (see the header).
+JDG_API int jdgpu_dfactor_export_levels(int* coupling_out, int* nlev_out, long long* nnzf_out, int* level_start,
+                                        long long* fp, int* fi, double* fx) {
+  const IldlcFactor<double>& F = G<double>().F;
+  *coupling_out = F.coupling;
+  *nlev_out = (int)F.level_start.size() - 1;
+  *nnzf_out = (long long)F.fi.size();
+  if (!level_start) return 0;
+  std::copy(F.level_start.begin(), F.level_start.end(), level_start);
+  if (F.coupling == 1) {
+    for (int i = 0; i <= F.n; ++i) fp[i] = F.fp[i];
+    std::copy(F.fi.begin(), F.fi.end(), fi);
+    std::copy(F.fx.begin(), F.fx.end(), fx);
+  }
+  return 0;
+}
+
 // The preconditioner application of jdgpu_dildl_apply without any GPU
 // memory allocation (see the header).  Returns 0, a factorisation error code,
 // -98 when the problem does not fit in the scratch array, -99 on a CUDA error.
@@ -1830,8 +2034,7 @@ JDG_API int jdgpu_dildl_apply_noalloc(int n, const int* ia, const int* ja, const
     p.droptol = droptol;
     p.condest = condest;
     p.mem = 0;
-    p.depth_weight = g_opt.depth_weight;
-    p.droptol_schur = g_opt.drop_schur;
+    factor_options(p, n);
     IldlcFactor<double> F;
     int ierr = ildlc_factor<double>(n, ia, ja, a, shift, nullptr, nullptr, nullptr, p, F);
     if (ierr) return ierr;
@@ -1843,9 +2046,10 @@ JDG_API int jdgpu_dildl_apply_noalloc(int n, const int* ia, const int* ja, const
     DevFactor<double> Fd;
     DevFactor<float> Fs;
     DevFactor<__nv_bfloat16> Fb;
-    if (precision == 1) upload_factor(F, Fs, st, bump);
-    else if (precision == 2) upload_factor(F, Fb, st, bump);
-    else upload_factor(F, Fd, st, bump);
+    // applied without the captured graph: no graph input/output vectors
+    if (precision == 1) upload_factor(F, Fs, st, bump, false);
+    else if (precision == 2) upload_factor(F, Fb, st, bump, false);
+    else upload_factor(F, Fd, st, bump, false);
     for (int r = 0; r < nrhs; ++r) {
       CK(cudaMemcpy(db, b + (size_t)r * n, sizeof(double) * n, cudaMemcpyHostToDevice));
       if (precision == 1) k::ildl_apply<double, float>(Fs, spd != 0, db, dx, st);
@@ -1890,6 +2094,13 @@ JDG_API void jdgpu_set_option(const char* name, double value) {
   else if (!std::strcmp(name, "revcom_device")) g_opt.revcom_device = (int)value;
   else if (!std::strcmp(name, "matching")) g_opt.matching = (int)value;
   else if (!std::strcmp(name, "verbose")) g_opt.verbose = (int)value;
+  else if (!std::strcmp(name, "coupling")) g_opt.coupling = (int)value;
+  else if (!std::strcmp(name, "drop_rule")) g_opt.drop_rule = (int)value;
+  else if (!std::strcmp(name, "last_droptol")) g_opt.last_droptol = value;
+  else if (!std::strcmp(name, "last_fill")) g_opt.last_fill = value;
+  else if (!std::strcmp(name, "coupled_min_n")) g_opt.coupled_min_n = (int)value;
+  else if (!std::strcmp(name, "lookahead")) g_opt.lookahead = (int)value;
+  else if (!std::strcmp(name, "factor_verbose")) g_opt.factor_verbose = (int)value;
 }
 
 // statistics of the last real-arithmetic solve: factor seconds, upload seconds,
@@ -1906,9 +2117,8 @@ JDG_API void jdgpu_dstats(double* out) {
   out[7] = (double)g.F.li.size();
   out[8] = g.F.fill();
   out[9] = g.nfactor;
-  out[10] = g.precision == 1 ? g.Fs.m_tail : g.precision == 2 ? g.Fb.m_tail : g.Fd.m_tail;
-  out[11] = (double)(g.precision == 1 ? g.Fs.blocks.size() : g.precision == 2 ? g.Fb.blocks.size()
-                                                                              : g.Fd.blocks.size());
+  out[10] = g.precision == 1 ? dense_rows(g.Fs) : g.precision == 2 ? dense_rows(g.Fb) : dense_rows(g.Fd);
+  out[11] = g.precision == 1 ? dense_blocks(g.Fs) : g.precision == 2 ? dense_blocks(g.Fb) : dense_blocks(g.Fd);
 }
 // the same for the complex solver state
 JDG_API void jdgpu_zstats(double* out) {
@@ -1923,9 +2133,8 @@ JDG_API void jdgpu_zstats(double* out) {
   out[7] = (double)g.F.li.size();
   out[8] = g.F.fill();
   out[9] = g.nfactor;
-  out[10] = g.precision == 1 ? g.Fs.m_tail : g.precision == 2 ? g.Fb.m_tail : g.Fd.m_tail;
-  out[11] = (double)(g.precision == 1 ? g.Fs.blocks.size() : g.precision == 2 ? g.Fb.blocks.size()
-                                                                              : g.Fd.blocks.size());
+  out[10] = g.precision == 1 ? dense_rows(g.Fs) : g.precision == 2 ? dense_rows(g.Fb) : dense_rows(g.Fd);
+  out[11] = g.precision == 1 ? dense_blocks(g.Fs) : g.precision == 2 ? dense_blocks(g.Fb) : dense_blocks(g.Fd);
 }
 JDG_API void jdgpu_reset_stats(void) {
   Global<double>& g = G<double>();
@@ -1955,8 +2164,7 @@ JDG_API int jdgpu_deigvec_grad(int n, const int* ia, const int* ja, const double
     p.droptol = droptol;
     p.condest = 5;
     p.mem = 0;
-    p.depth_weight = g_opt.depth_weight;
-    p.droptol_schur = g_opt.drop_schur;
+    factor_options(p, n);
     IldlcFactor<double> F;
     int ierr;
     if (bdiag) {  // A - lambda B with B diagonal: B as its own diagonal CSR

@@ -29,6 +29,8 @@
 #include <complex>
 #include <cstdint>
 #include <atomic>
+#include <chrono>
+#include <cstdio>
 #include <cstring>
 #include <functional>
 #include <thread>
@@ -61,6 +63,25 @@ struct IldlcParams {
   double dense_max_bytes = 16e9;  //   and its dense copy fits in this many bytes
   int matching = 0;            // 1: first level's decisions use the maximum-product matching scale;
                                // 2: also pivot matched 2-cycles of that level as 2x2 blocks first
+  int coupling = 0;            // 0: one global unit L; the rows of deferred nodes keep their entries
+                               //    in the columns of earlier levels (L21 = E B^{-1}, dropped);
+                               // 1: per level, the coupling block F of the level's matrix (as in
+                               //    ILUPACK's multilevel form, symAMGsol.c:173-330): L holds only the
+                               //    entries inside each level, and an application solves with B twice
+  double last_droptol = -1;    // drop tolerance of the last level (<0: droptol; 0: the last level is
+                               // factored without dropping, like ILUPACK's dense last level,
+                               // symAMGsetup.c:450-560); its Schur fill threshold is a tenth of it
+  double last_fill = 0;        // > 0: a later level whose matrix is at least this fraction full becomes
+                               // the last level (ILUPACK switches at one third)
+  int lookahead = 0;           // 1: also defer a pivot whose kept column would raise a neighbour's
+                               //    inverse estimate above condest (ILUPACK's improved estimate,
+                               //    sympiluc.F:1440-1510: the pivot is skipped, not its neighbours)
+  int verbose = 0;             // 1: one line per level on stderr (rows, accepted, entries, seconds)
+  int drop_rule = 0;           // 0: drop l_ik when |l_ik| |e_k^T L^{-1}| <= droptol;
+                               // 1: drop l_ik when its largest rank-1 term in the Schur complement,
+                               //    |l_ik| |d_k| max_m |l_mk| (scaled), is <= droptol / kmax, kmax the
+                               //    largest inverse estimate accepted so far in the level (the rule of
+                               //    ILUPACK's sympiluc.F:2187-2240 with IMPROVED_ESTIMATE)
 };
 
 template <class T> struct IldlcFactor {
@@ -76,7 +97,17 @@ template <class T> struct IldlcFactor {
   std::vector<int> level_start; // elimination steps where each level starts, plus n
   int nneg = 0;                 // negative eigenvalues of D (pivots converted by |D|)
   int64_t nnz_a_upper = 0;
-  double fill() const { return (double)(li.size() + (size_t)n) / (double)std::max<int64_t>(1, nnz_a_upper); }
+  // coupling == 1: per level l, the block F_l = S_l(B_l, C_l) of the level's matrix S_l between the
+  // pivots accepted in the level (rows, elimination steps) and the nodes deferred from it (columns,
+  // elimination steps of later levels); L has no entries across levels.  The preconditioner is
+  //   M_l = [B_l  F_l; F_l^H  S_{l+1} + F_l^H B_l^{-1} F_l],  B_l = L_l D_l L_l^H.
+  int coupling = 0;
+  std::vector<int64_t> fp;      // CSR rows of F over all elimination steps (empty rows outside B_l)
+  std::vector<int> fi;
+  std::vector<T> fx;
+  double fill() const {
+    return (double)(li.size() + fi.size() + (size_t)n) / (double)std::max<int64_t>(1, nnz_a_upper);
+  }
 };
 
 namespace detail {
@@ -273,7 +304,17 @@ int ildlc_factor(int n, const int* ia, const int* ja, const T* a, double shift, 
   }
 
   const double dropS = prm.droptol_schur >= 0 ? prm.droptol_schur : prm.droptol * 0.1;
+  // drop thresholds of the current level (the last level may keep more, see last_droptol)
+  double lvl_droptol = prm.droptol, lvl_dropS = dropS;
   const double kappa = prm.condest;
+  double kmax_lvl = 1.0;  // largest inverse estimate accepted in the current level (drop_rule 1)
+  // drop_rule 1: threshold on the scaled |l| of a column whose scaled pivot
+  // magnitude is dsc and whose largest scaled entry is lmx
+  auto crule_thr = [&](double nu, double dsc, double lmx) {
+    kmax_lvl = std::max(kmax_lvl, nu);
+    const double c = dsc * lmx;
+    return c > 0 ? lvl_droptol / (kmax_lvl * c) : 0.0;
+  };
   F = IldlcFactor<T>();
   F.n = n;
   F.nnz_a_upper = nnzu;
@@ -291,6 +332,21 @@ int ildlc_factor(int n, const int* ia, const int* ja, const T* a, double shift, 
   crow.reserve((size_t)nnzu * 3);
   cval.reserve((size_t)nnzu * 3);
   const int64_t memcap = prm.mem > 0 ? (int64_t)(prm.mem * (double)nnzu) : INT64_MAX;
+  const bool fform = prm.coupling == 1;
+  // coupling 1: entries stored by the finished levels (their L and F), the
+  // column entries at the start of the current level, the level's matrix
+  // S_l(i, j) (i < j, node ids) and the F entries (accepted row, deferred column)
+  int64_t stored_done = 0, crow_lvl0 = 0;
+  struct Trip { int r, c; T v; };
+  std::vector<Trip> snap, fent;
+  std::vector<int> node_level(n, 0);
+  // within a level, the column entries of L include those of the deferred rows
+  // (E B^{-1}, not stored with coupling 1): a guard against runaway fill
+  auto over_mem = [&]() {
+    if (!fform) return (int64_t)crow.size() + n > memcap;
+    const int64_t cur = stored_done + ((int64_t)crow.size() - crow_lvl0) + (int64_t)fent.size();
+    return memcap < INT64_MAX / 4 && cur + n > 3 * memcap;
+  };
 
   std::vector<char> state(n, 0);  // 0 active candidate, 1 eliminated, 2 deferred
   std::vector<double> sc(n, 1.0), xi(n, 0.0);
@@ -387,7 +443,7 @@ int ildlc_factor(int n, const int* ia, const int* ja, const T* a, double shift, 
           if (u == T(0)) continue;
           if (row[c] != T(0)) {
             row[c] -= u;
-          } else if (fab(u) * sr * s[c] > dropS) {
+          } else if (fab(u) * sr * s[c] > lvl_dropS) {
             row[c] = -u;
             cnt[r]++;
           }
@@ -447,6 +503,14 @@ int ildlc_factor(int n, const int* ia, const int* ja, const T* a, double shift, 
         const T d = at(tp, tp);
         const double nx = last_lvl ? 1.0 : nu_of(kk);
         const double sp = s[tp];
+        const bool crule = prm.drop_rule == 1 && !last_lvl;
+        double cthr = 0;
+        if (crule) {
+          double lmx = 0;
+          for (int r = 0; r < m; ++r)
+            if (r != tp && st[r] != 1 && at(r, tp) != T(0)) lmx = std::max(lmx, fab(at(r, tp) / d) * s[r] / sp);
+          cthr = crule_thr(nx, fab(d) * sp * sp, lmx);
+        }
         kr.clear();
         std::fill(lf.begin(), lf.end(), T(0));
         for (int r = 0; r < m; ++r) {
@@ -454,7 +518,7 @@ int ildlc_factor(int n, const int* ia, const int* ja, const T* a, double shift, 
           const T a_rk = at(r, tp);
           if (a_rk == T(0)) continue;
           const T l = a_rk / d;
-          if (fab(l) * s[r] / sp * nx <= prm.droptol) continue;
+          if (crule ? fab(l) * s[r] / sp <= cthr : fab(l) * s[r] / sp * nx <= lvl_droptol) continue;
           lf[r] = l;
           kr.push_back(r);
         }
@@ -507,10 +571,22 @@ int ildlc_factor(int n, const int* ia, const int* ja, const T* a, double shift, 
         if (!last_lvl && (!ok || lmax > kappa)) { st[t] = 2; state[k] = 2; deferred.push_back(k); continue; }
         if (last_lvl && !(fab(det) > 0)) return (int)order.size() + 1;
         const double nxk = last_lvl ? 1.0 : nu_of(k), nxj = last_lvl ? 1.0 : nu_of(j);
+        const bool crule = prm.drop_rule == 1 && !last_lvl;
+        double thk = 0, thj = 0;
+        if (crule) {
+          double mk = 0, mj = 0;
+          for (int r : nb) {
+            mk = std::max(mk, fab(lf[r]) * s[r] / skt);
+            mj = std::max(mj, fab(lg[r]) * s[r] / sj);
+          }
+          const double bd = std::max({fab(dkk) * skt * skt, fab(djj) * sj * sj, fab(akj) * skt * sj});
+          thk = crule_thr(nxk, bd, mk);
+          thj = crule_thr(nxj, bd, mj);
+        }
         kr.clear();
         for (int r : nb) {
-          if (fab(lf[r]) * s[r] / skt * nxk <= prm.droptol) lf[r] = T(0);
-          if (fab(lg[r]) * s[r] / sj * nxj <= prm.droptol) lg[r] = T(0);
+          if (crule ? fab(lf[r]) * s[r] / skt <= thk : fab(lf[r]) * s[r] / skt * nxk <= lvl_droptol) lf[r] = T(0);
+          if (crule ? fab(lg[r]) * s[r] / sj <= thj : fab(lg[r]) * s[r] / sj * nxj <= lvl_droptol) lg[r] = T(0);
           if (lf[r] != T(0) || lg[r] != T(0)) kr.push_back(r);
         }
         if (!last_lvl) {
@@ -559,7 +635,7 @@ int ildlc_factor(int n, const int* ia, const int* ja, const T* a, double shift, 
         state[j] = 1;
         accepted += 2;
       }
-      if ((int64_t)crow.size() + n > memcap) return -3;
+      if (over_mem()) return -3;
       for (int r : kr)
         if (st[r] == 0) DQ.update(r, dkey(r));
     }
@@ -575,6 +651,7 @@ int ildlc_factor(int n, const int* ia, const int* ja, const T* a, double shift, 
     return 0;
   };
 
+  double t_level0 = std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
   while (!level_nodes.empty()) {
     const int nl = (int)level_nodes.size();
     if (level >= prm.max_levels || nl <= prm.last_level_min) last = true;
@@ -620,13 +697,30 @@ int ildlc_factor(int n, const int* ia, const int* ja, const T* a, double shift, 
     }
     std::vector<int> deferred;
     int accepted_here = 0;
+    kmax_lvl = 1.0;
     int64_t level_entries = 0;
     for (int i : level_nodes) {
       xi[i] = 0;
       xic[i] = 0;
       state[i] = 0;
       level_entries += (int64_t)A.rows[i].size();
+      node_level[i] = level;
     }
+    if (fform) {
+      // the level's matrix before its elimination: F is its accepted x deferred block
+      crow_lvl0 = (int64_t)crow.size();
+      snap.clear();
+      for (int i : level_nodes) {
+        dlev[i] = 0;  // levels have no dependencies across them
+        for (auto& e : A.rows[i])
+          if (i < e.col) snap.push_back({i, e.col, e.val});
+      }
+    }
+    if (!last && level > 0 && prm.last_fill > 0 &&
+        (double)level_entries >= prm.last_fill * (double)nl * (double)(nl - 1))
+      last = true;
+    lvl_droptol = (last && prm.last_droptol >= 0) ? prm.last_droptol : prm.droptol;
+    lvl_dropS = (last && prm.last_droptol >= 0) ? 0.1 * prm.last_droptol : dropS;
     const bool dense_lvl = nl >= prm.dense_min_rows &&
                            (double)level_entries >= prm.dense_fill * (double)nl * (double)(nl - 1) &&
                            (double)nl * (double)nl * sizeof(T) <= prm.dense_max_bytes;
@@ -699,17 +793,42 @@ int ildlc_factor(int n, const int* ia, const int* ja, const T* a, double shift, 
         // 1x1 pivot at k
         T d = dk;
         double nx = last ? 1.0 : nuk;
+        const bool crule = prm.drop_rule == 1 && !last;
+        double cthr = 0;
+        if (crule) {
+          double lmx = 0;
+          for (auto& e : A.rows[k])
+            if (state[e.col] != 1) lmx = std::max(lmx, fab(fcj(e.val) / d) * sc[e.col] / skk);
+          cthr = crule_thr(nx, fab(d) * skk * skk, lmx);
+        }
         kept.clear();
         lk.clear();
         for (auto& e : A.rows[k]) {
           if (state[e.col] == 1) continue;
           T l = fcj(e.val) / d;  // L(i,k) = A(i,k)/d, A(i,k) = conj(A(k,i))
           double ls = fab(l) * sc[e.col] / skk;
-          if (ls * nx <= prm.droptol) continue;
+          if (crule ? ls <= cthr : ls * nx <= lvl_droptol) continue;
           kept.push_back(e.col);
           lk.push_back(l);
         }
         // (the row of every neighbour loses column k below)
+        if (!last && prm.lookahead) {
+          bool over = false;
+          if (is_cplx) {
+            cplx x = (std::abs(xic[k]) > 0) ? -xic[k] / std::abs(xic[k]) * (1 + std::abs(xic[k])) : cplx(1);
+            for (size_t q = 0; q < kept.size() && !over; ++q)
+              over = std::abs(xic[kept[q]] + cplx(lk[q] * T(sc[kept[q]] / skk)) * x) > kappa;
+          } else {
+            double x = (xi[k] != 0) ? -(xi[k] / std::fabs(xi[k])) * (1 + std::fabs(xi[k])) : 1.0;
+            for (size_t q = 0; q < kept.size() && !over; ++q)
+              over = std::fabs(xi[kept[q]] + fre(lk[q]) * (sc[kept[q]] / skk) * x) > kappa;
+          }
+          if (over) {
+            state[k] = 2;
+            deferred.push_back(k);
+            continue;
+          }
+        }
         if (!last) {
           // estimator: choose x_k to maximise growth
           if (is_cplx) {
@@ -764,7 +883,7 @@ int ildlc_factor(int n, const int* ia, const int* ja, const T* a, double shift, 
             int j = kept[t];
             T u = lid * fcj(lk[t]);
             if (ps[j].stamp == stamp) row[ps[j].pos].val -= u;
-            else if (fab(u) * sc[i] * sc[j] > dropS) {
+            else if (fab(u) * sc[i] * sc[j] > lvl_dropS) {
               row.push_back({j, -u});
               ps[j] = PosStamp{stamp, (int)row.size() - 1};
             }
@@ -830,13 +949,48 @@ int ildlc_factor(int n, const int* ia, const int* ja, const T* a, double shift, 
         }
         if (last && !(fab(det) > 0)) return (int)order.size() + 1;
         double nxk = last ? 1.0 : nu_of(k), nxj = last ? 1.0 : nu_of(j);
+        const bool crule = prm.drop_rule == 1 && !last;
+        double thk = 0, thj = 0;
+        if (crule) {
+          double mk = 0, mj = 0;
+          for (size_t q = 0; q < nb.size(); ++q) {
+            mk = std::max(mk, fab(lk[q]) * sc[nb[q]] / skk);
+            mj = std::max(mj, fab(lj[q]) * sc[nb[q]] / sj);
+          }
+          const double bd = std::max({fab(dkk) * skk * skk, fab(djj) * sj * sj, fab(akj) * skk * sj});
+          thk = crule_thr(nxk, bd, mk);
+          thj = crule_thr(nxj, bd, mj);
+        }
         // dropping per entry
         std::vector<char> keepk(nb.size()), keepj(nb.size());
         for (size_t q = 0; q < nb.size(); ++q) {
-          keepk[q] = fab(lk[q]) * sc[nb[q]] / skk * nxk > prm.droptol;
-          keepj[q] = fab(lj[q]) * sc[nb[q]] / sj * nxj > prm.droptol;
+          keepk[q] = crule ? fab(lk[q]) * sc[nb[q]] / skk > thk : fab(lk[q]) * sc[nb[q]] / skk * nxk > lvl_droptol;
+          keepj[q] = crule ? fab(lj[q]) * sc[nb[q]] / sj > thj : fab(lj[q]) * sc[nb[q]] / sj * nxj > lvl_droptol;
           if (!keepk[q]) lk[q] = T(0);
           if (!keepj[q]) lj[q] = T(0);
+        }
+        if (!last && prm.lookahead) {
+          bool over = false;
+          if (is_cplx) {
+            cplx xk = (std::abs(xic[k]) > 0) ? -xic[k] / std::abs(xic[k]) * (1 + std::abs(xic[k])) : cplx(1);
+            cplx xj = (std::abs(xic[j]) > 0) ? -xic[j] / std::abs(xic[j]) * (1 + std::abs(xic[j])) : cplx(1);
+            for (size_t q = 0; q < nb.size() && !over; ++q) {
+              const int i = nb[q];
+              over = std::abs(xic[i] + cplx(lk[q] * T(sc[i] / skk)) * xk + cplx(lj[q] * T(sc[i] / sj)) * xj) > kappa;
+            }
+          } else {
+            double xk = (xi[k] != 0) ? -(xi[k] / std::fabs(xi[k])) * (1 + std::fabs(xi[k])) : 1.0;
+            double xj = (xi[j] != 0) ? -(xi[j] / std::fabs(xi[j])) * (1 + std::fabs(xi[j])) : 1.0;
+            for (size_t q = 0; q < nb.size() && !over; ++q) {
+              const int i = nb[q];
+              over = std::fabs(xi[i] + fre(lk[q]) * (sc[i] / skk) * xk + fre(lj[q]) * (sc[i] / sj) * xj) > kappa;
+            }
+          }
+          if (over) {
+            state[k] = 2;
+            deferred.push_back(k);
+            continue;
+          }
         }
         if (!last) {
           if (is_cplx) {
@@ -877,7 +1031,7 @@ int ildlc_factor(int n, const int* ia, const int* ja, const T* a, double shift, 
             T u = lk[qa] * t0 + lj[qa] * t1;
             if (l == i) { A.diag[i] -= T(fre(u)); continue; }
             if (ps[l].stamp == stamp) row[ps[l].pos].val -= u;
-            else if (fab(u) * sc[i] * sc[l] > dropS) {
+            else if (fab(u) * sc[i] * sc[l] > lvl_dropS) {
               row.push_back({l, -u});
               ps[l] = PosStamp{stamp, (int)row.size() - 1};
             }
@@ -918,10 +1072,29 @@ int ildlc_factor(int n, const int* ia, const int* ja, const T* a, double shift, 
         deferred.push_back(k);
         continue;
       }
-      if ((int64_t)crow.size() + n > memcap) return -3;
+      if (over_mem()) return -3;
       // degree updates of the touched rows
       for (int i : kept)
         if (state[i] == 0) Q.update(i, qkey(i));
+    }
+    if (prm.verbose) {
+      const double now = std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+      std::fprintf(stderr, "ildlc level %d: %d rows (%s%s), %d accepted, %lld level entries, L %lld, %.1f s\n",
+                   level, nl, last ? "last" : "deferring", dense_lvl ? ", dense" : "", accepted_here,
+                   (long long)level_entries, (long long)crow.size(), now - t_level0);
+      t_level0 = now;
+    }
+    if (fform) {
+      for (auto& t : snap) {
+        if (state[t.r] == 1 && state[t.c] == 2) fent.push_back(t);
+        else if (state[t.r] == 2 && state[t.c] == 1) fent.push_back({t.c, t.r, fcj(t.v)});
+      }
+      snap.clear();
+      snap.shrink_to_fit();
+      // stored: the L entries between this level's accepted rows
+      for (int64_t q = crow_lvl0; q < (int64_t)crow.size(); ++q)
+        if (state[crow[q]] == 1) stored_done++;
+      if (stored_done + (int64_t)fent.size() + n > memcap) return -3;
     }
     level++;
     if (deferred.empty()) break;
@@ -934,9 +1107,13 @@ int ildlc_factor(int n, const int* ia, const int* ja, const T* a, double shift, 
   F.blk = blk;
   F.dinv = dinv;
   F.doff = doff;
+  F.coupling = fform ? 1 : 0;
+  // coupling 1 keeps only the entries inside a level (column step p and its rows in the same level)
+  auto keep_entry = [&](int p, int r) { return !fform || node_level[order[p]] == node_level[order[r]]; };
   std::vector<int64_t> rc(n + 1, 0);
   for (int p = 0; p < n; ++p)
-    for (int64_t q = colptr[p]; q < colptr[p + 1]; ++q) rc[pos[crow[q]] + 1]++;
+    for (int64_t q = colptr[p]; q < colptr[p + 1]; ++q)
+      if (keep_entry(p, pos[crow[q]])) rc[pos[crow[q]] + 1]++;
   for (int p = 0; p < n; ++p) rc[p + 1] += rc[p];
   F.lp = rc;
   F.li.assign(rc[n], 0);
@@ -945,10 +1122,36 @@ int ildlc_factor(int n, const int* ia, const int* ja, const T* a, double shift, 
   for (int p = 0; p < n; ++p)
     for (int64_t q = colptr[p]; q < colptr[p + 1]; ++q) {
       int r = pos[crow[q]];
+      if (!keep_entry(p, r)) continue;
       F.li[fillp[r]] = p;
       F.lx[fillp[r]] = cval[q];
       fillp[r]++;
     }
+  if (fform) {
+    // F in CSR over elimination steps, columns ascending within a row
+    F.fp.assign(n + 1, 0);
+    for (auto& t : fent) F.fp[pos[t.r] + 1]++;
+    for (int p = 0; p < n; ++p) F.fp[p + 1] += F.fp[p];
+    F.fi.assign(fent.size(), 0);
+    F.fx.assign(fent.size(), T(0));
+    std::vector<int64_t> fq(F.fp.begin(), F.fp.end() - 1);
+    for (auto& t : fent) {
+      const int64_t q = fq[pos[t.r]]++;
+      F.fi[q] = pos[t.c];
+      F.fx[q] = t.v;
+    }
+    for (int p = 0; p < n; ++p) {
+      std::vector<std::pair<int, T>> row;
+      for (int64_t q = F.fp[p]; q < F.fp[p + 1]; ++q) row.push_back({F.fi[q], F.fx[q]});
+      std::sort(row.begin(), row.end(), [](const std::pair<int, T>& x, const std::pair<int, T>& y) {
+        return x.first < y.first;
+      });
+      for (size_t t = 0; t < row.size(); ++t) {
+        F.fi[F.fp[p] + t] = row[t].first;
+        F.fx[F.fp[p] + t] = row[t].second;
+      }
+    }
+  }
   // |D|^{-1} (SPD conversion) and the count of negative eigenvalues of D
   F.ainv.assign(n, T(0));
   F.aoff.assign(n, T(0));

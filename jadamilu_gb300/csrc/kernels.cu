@@ -234,7 +234,7 @@ constexpr int GMV_MAX = 64;
 template <class T> struct SmallVec { T v[GMV_MAX]; };
 
 template <class T>
-__global__ void __launch_bounds__(TPB) gemv_dev_kernel(long n, int k, T alpha, const T* __restrict__ V, long ldv,
+__global__ void __launch_bounds__(TPB) jd_basis_gemv_dev_kernel(long n, int k, T alpha, const T* __restrict__ V, long ldv,
                                                        const T* __restrict__ y, T beta, T* __restrict__ w) {
   pdl_begin();
   __shared__ T ys[GMV_MAX];
@@ -248,7 +248,7 @@ __global__ void __launch_bounds__(TPB) gemv_dev_kernel(long n, int k, T alpha, c
   }
 }
 template <class T>
-__global__ void __launch_bounds__(TPB) gemv_val_kernel(long n, int k, T alpha, const T* __restrict__ V, long ldv,
+__global__ void __launch_bounds__(TPB) jd_basis_gemv_val_kernel(long n, int k, T alpha, const T* __restrict__ V, long ldv,
                                                        SmallVec<T> y, T beta, T* __restrict__ w) {
   pdl_begin();
   for (long i = blockIdx.x * (long)TPB + threadIdx.x; i < n; i += (long)gridDim.x * TPB) {
@@ -268,7 +268,7 @@ void gemv_dev(long n, int k, T alpha, const T* V, long ldv, const T* y, T beta, 
     }
     return;
   }
-  launch_k(gemv_dev_kernel<T>, dim3(grid_1d(n)), dim3(TPB), 0, s, n, k, alpha, V, ldv, y, beta, w);
+  launch_k(jd_basis_gemv_dev_kernel<T>, dim3(grid_1d(n)), dim3(TPB), 0, s, n, k, alpha, V, ldv, y, beta, w);
   COUNT_LAUNCH();
 }
 template <class T>
@@ -280,17 +280,20 @@ void gemv_val(long n, int k, T alpha, const T* V, long ldv, const T* yh, T beta,
   }
   SmallVec<T> y;
   for (int c = 0; c < k; ++c) y.v[c] = yh[c];
-  launch_k(gemv_val_kernel<T>, dim3(grid_1d(n)), dim3(TPB), 0, s, n, k, alpha, V, ldv, y, beta, w);
+  launch_k(jd_basis_gemv_val_kernel<T>, dim3(grid_1d(n)), dim3(TPB), 0, s, n, k, alpha, V, ldv, y, beta, w);
   COUNT_LAUNCH();
 }
 
+// Q (K x keep, leading dimension K, K <= 32) travels in the kernel's
+// parameters: at most 16 KB for complex<double>, inside the 32 KB parameter
+// space, so a restart needs no staging copy and no host synchronisation.
 template <class T> struct SmallMat { T q[32 * 32]; };
 template <class T>
 __global__ void __launch_bounds__(TPB) rmult_kernel(long n, int K, int keep, const T* __restrict__ V, long ldv,
-                                                    const T* __restrict__ Q, T* __restrict__ out) {
+                                                    const __grid_constant__ SmallMat<T> Q, T* __restrict__ out) {
   pdl_begin();
   __shared__ T qs[32 * 32];
-  for (int t = threadIdx.x; t < K * keep; t += TPB) qs[t] = Q[t];
+  for (int t = threadIdx.x; t < K * keep; t += TPB) qs[t] = Q.q[t];
   __syncthreads();
   for (long i = blockIdx.x * (long)TPB + threadIdx.x; i < n; i += (long)gridDim.x * TPB) {
     T row[32];
@@ -303,16 +306,11 @@ __global__ void __launch_bounds__(TPB) rmult_kernel(long n, int K, int keep, con
   }
 }
 template <class T> void rmult(long n, int K, int keep, const T* V, long ldv, const T* Qh, T* out, cudaStream_t s) {
-  if (K > 32) throw std::runtime_error("rmult: search space above 32");
-  // Q travels through a small device staging area owned by the kernel launch
-  static thread_local T* dq = nullptr;
-  if (!dq) CK(cudaMalloc(&dq, sizeof(T) * 32 * 32));
-  std::vector<T> q(K * keep);
+  if (K > 32 || keep > K) throw std::runtime_error("rmult: search space above 32");
+  SmallMat<T> q;
   for (int c = 0; c < keep; ++c)
-    for (int kk = 0; kk < K; ++kk) q[kk + c * K] = Qh[kk + c * K];
-  CK(cudaMemcpyAsync(dq, q.data(), sizeof(T) * K * keep, cudaMemcpyHostToDevice, s));
-  CK(cudaStreamSynchronize(s));  // the pageable source must not change before the copy
-  launch_k(rmult_kernel<T>, dim3(grid_1d(n)), dim3(TPB), 0, s, n, K, keep, V, ldv, dq, out);
+    for (int kk = 0; kk < K; ++kk) q.q[kk + c * K] = Qh[kk + c * K];
+  launch_k(rmult_kernel<T>, dim3(grid_1d(n)), dim3(TPB), 0, s, n, K, keep, V, ldv, q, out);
   COUNT_LAUNCH();
 }
 
@@ -420,6 +418,7 @@ constexpr int WIDE_TPB = 256;
 static inline int lanes_for(double entries_per_row) {
   return entries_per_row >= 48 ? 32 : entries_per_row >= 20 ? 16 : 8;
 }
+int lanes_per_row(double entries_per_row) { return lanes_for(entries_per_row); }
 template <class S, class A, int LANES>
 __global__ void __launch_bounds__(WIDE_TPB) ildl_wide_kernel(int lo, int hi, const int* __restrict__ rows,
                                                             const int64_t* __restrict__ rp, const int* __restrict__ ci,
@@ -678,12 +677,17 @@ __global__ void __cluster_dims__(TRI_CL, 1, 1) __launch_bounds__(TRI_TPB)
 // raise the dynamic shared-memory limit of the tail kernel once per size
 // (done before any graph capture: ildl_apply_graph calls it first)
 template <class S, class A> static void ensure_tail_smem(size_t bytes) {
+  // the attribute applies to the current device only: one raised size per device
+  constexpr int kMaxDev = 64;
   static std::mutex mu;
-  static size_t set = 48 * 1024;
+  static size_t set[kMaxDev] = {};
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
   std::lock_guard<std::mutex> lk(mu);
-  if (bytes > set) {
+  size_t& cur = set[dev < kMaxDev ? dev : kMaxDev - 1];
+  if (dev >= kMaxDev || bytes > std::max<size_t>(cur, 48 * 1024)) {
     CK(cudaFuncSetAttribute(tail_run_kernel<S, A>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-    set = bytes;
+    cur = std::max(cur, bytes);
   }
 }
 
@@ -743,9 +747,81 @@ template <class S> void ildl_plan_bwd0(DevFactor<S>& F, const std::vector<int64_
   F.bseg = seg;
 }
 
+// Coupling blocks of the multilevel form (symAMGsol.c:173-330 applies them
+// with CSRMATVEC / CSRMATTVEC): the m rows of a CSR block (row pointers rp[t],
+// t < m, global columns) written to y[r0 + t], LANES lanes per row, in the
+// outer precision T.  SUB: y[r0 + t] -= sum_q v_q x[c_q]; else
+// y[r0 + t] = sum_q v_q x[c_q].  The rows written and the columns read are
+// disjoint ranges, so x may alias y.
+template <class T, class S, int LANES, bool SUB>
+__global__ void __launch_bounds__(WIDE_TPB) couple_kernel(int r0, int m, const int64_t* __restrict__ rp,
+                                                         const int* __restrict__ ci, const S* __restrict__ cv,
+                                                         const T* x, T* y) {
+  pdl_begin();
+  const int t = blockIdx.x * (WIDE_TPB / LANES) + (threadIdx.x / LANES);
+  const int lane = threadIdx.x % LANES;
+  const int r = r0 + t;
+  T acc = T(0);
+  if (t < m)
+    for (int64_t q = rp[t] + lane; q < rp[t + 1]; q += LANES) acc = fma_(cvt<T>(ld_arith(cv + q)), x[ci[q]], acc);
+  for (int o = LANES / 2; o > 0; o >>= 1) acc = acc + shfl_xor_any(acc, o);
+  if (t < m && lane == 0) y[r] = SUB ? y[r] - acc : acc;
+}
+template <class T, class S, bool SUB>
+static void launch_couple(int lanes, int r0, int m, const int64_t* rp, const int* ci, const S* cv, const T* x, T* y,
+                          cudaStream_t s) {
+  if (m <= 0) return;
+  const int nb = m * lanes / WIDE_TPB + 1;
+  if (lanes == 32) launch_k(couple_kernel<T, S, 32, SUB>, dim3(nb), dim3(WIDE_TPB), 0, s, r0, m, rp, ci, cv, x, y);
+  else if (lanes == 16) launch_k(couple_kernel<T, S, 16, SUB>, dim3(nb), dim3(WIDE_TPB), 0, s, r0, m, rp, ci, cv, x, y);
+  else launch_k(couple_kernel<T, S, 8, SUB>, dim3(nb), dim3(WIDE_TPB), 0, s, r0, m, rp, ci, cv, x, y);
+}
+// y[r] = yb[r] - t[r] for r in [r0, r0 + m)
+template <class T>
+__global__ void couple_combine_kernel(int r0, int m, const T* __restrict__ yb, const T* __restrict__ t, T* __restrict__ y) {
+  pdl_begin();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < m) y[r0 + i] = yb[r0 + i] - t[r0 + i];
+}
+
+template <class T, class S> void ildl_apply(const DevFactor<S>& F, bool spd, const T* b, T* x, cudaStream_t s);
+
+// The multilevel application with coupling blocks: per level l with rows B
+// (steps [a, e)) and the later rows C,
+//   forward:  y_B = B^{-1} y_B (the level's sub-factor), keep it, y_C -= F^H y_B;
+//   backward: t_B = B^{-1} (F y_C), y_B = kept y_B - t_B.
+template <class T, class S>
+static void ildl_apply_coupled(const DevFactor<S>& F, bool spd, const T* b, T* x, cudaStream_t s) {
+  const int n = F.n;
+  const int nl = (int)F.lev.size();
+  T* y = (T*)F.cy;
+  T* yb = (T*)F.cyb;
+  T* t = (T*)F.ct;
+  launch_k(ildl_gather_kernel<T, T>, dim3(nblk(n)), dim3(TPB), 0, s, n, F.perm, b, y);
+  for (int l = 0; l < nl; ++l) {
+    const int a = F.lstart[l], e = F.lstart[l + 1];
+    ildl_apply<T, S>(F.lev[l], spd, y + a, y + a, s);
+    if (l + 1 < nl) {
+      CK(cudaMemcpyAsync(yb + a, y + a, sizeof(T) * (size_t)(e - a), cudaMemcpyDeviceToDevice, s));
+      launch_couple<T, S, true>(F.fh_lanes[l], e, n - e, F.fhp + F.fh_row0[l], F.fhi, F.fhx, y, y, s);
+    }
+  }
+  for (int l = nl - 2; l >= 0; --l) {
+    const int a = F.lstart[l], e = F.lstart[l + 1];
+    launch_couple<T, S, false>(F.fp_lanes[l], a, e - a, F.fpp + a, F.fpi, F.fpx, y, t, s);
+    ildl_apply<T, S>(F.lev[l], spd, t + a, t + a, s);
+    launch_k(couple_combine_kernel<T>, dim3(nblk(e - a)), dim3(TPB), 0, s, a, e - a, (const T*)yb, (const T*)t, y);
+  }
+  launch_k(ildl_scatter_kernel<T, T>, dim3(nblk(n)), dim3(TPB), 0, s, n, F.perm, (const T*)y, x);
+}
+
 template <class T, class S> void ildl_apply(const DevFactor<S>& F, bool spd, const T* b, T* x, cudaStream_t s) {
   using A = typename Arith<S>::type;
   const int n = F.n;
+  if (F.coupled) {
+    ildl_apply_coupled<T, S>(F, spd, b, x, s);
+    return;
+  }
   launch_k(ildl_gather_kernel<T, A>, dim3(nblk(n)), dim3(TPB), 0, s, n, F.orig, b, F.y);
   auto sweep = [&](const std::vector<int>& seg, const std::vector<int>& ptr, const int* dptr, const int* rows,
                    const int64_t* rp, const int* ci, const S* cv) {
@@ -810,9 +886,13 @@ template <class T, class S> void ildl_apply_graph(DevFactor<S>& F, bool spd, con
   const int g = spd ? 1 : 0;
   if (!F.graph[g]) {
     using A = typename Arith<S>::type;
-    if (F.m_tail > 0 && F.blocks.empty())
-      ensure_tail_smem<S, A>(std::max(tail_smem_bytes<A>(F.m_tail, (int)F.tfptr.size() - 1, false),
-                                      tail_smem_bytes<A>(F.m_tail, (int)F.tbptr.size() - 1, true)));
+    auto smem = [](const DevFactor<S>& D) {
+      if (D.m_tail > 0 && D.blocks.empty())
+        ensure_tail_smem<S, A>(std::max(tail_smem_bytes<A>(D.m_tail, (int)D.tfptr.size() - 1, false),
+                                        tail_smem_bytes<A>(D.m_tail, (int)D.tbptr.size() - 1, true)));
+    };
+    smem(F);
+    for (const auto& D : F.lev) smem(D);
     cudaGraph_t gr;
     CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     ildl_apply<T, S>(F, spd, (const T*)F.rhs_in, (T*)F.sol_out, s);
@@ -858,14 +938,6 @@ JD_INST_F(double, __nv_bfloat16)
 JD_INST_F(zc, zc)
 JD_INST_F(zc, cc)
 JD_INST_F(zc, bc)
-#if 0
-template void ildl_apply<double, double>(const DevFactor<double>&, bool, const double*, double*, cudaStream_t);
-template void ildl_apply<double, float>(const DevFactor<float>&, bool, const double*, double*, cudaStream_t);
-template void ildl_apply<double, __nv_bfloat16>(const DevFactor<__nv_bfloat16>&, bool, const double*, double*, cudaStream_t);
-template void ildl_apply<zc, zc>(const DevFactor<zc>&, bool, const zc*, zc*, cudaStream_t);
-template void ildl_apply<zc, cc>(const DevFactor<cc>&, bool, const zc*, zc*, cudaStream_t);
-template void ildl_apply<zc, bc>(const DevFactor<bc>&, bool, const zc*, zc*, cudaStream_t);
-#endif
 
 }  // namespace k
 }  // namespace jdg

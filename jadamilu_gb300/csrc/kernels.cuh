@@ -80,6 +80,23 @@ template <class S> struct DevFactor {
   long long graph_kernels[2] = {0, 0};
   void* rhs_in = nullptr;
   void* sol_out = nullptr;
+  // Multilevel form with coupling blocks (IldlcFactor::coupling == 1): one
+  // sub-factor per level (rows in elimination order, identity permutation),
+  // the blocks F (rows: steps of the level's pivots; columns: later steps;
+  // one CSR over all steps) and, per level l, F_l^H (rows: the steps after
+  // level l, row pointers from fhp + fh_row0[l]; columns: the level's steps),
+  // and three outer-precision work vectors of n entries.  The fields above
+  // then hold only n, nnz_l, graph and the graph's input/output vectors.
+  int coupled = 0;
+  std::vector<DevFactor<S>> lev;
+  std::vector<int> lstart;                   // first step of each level, plus n
+  int* perm = nullptr;                       // elimination step -> row of the input vector
+  int64_t* fpp = nullptr; int* fpi = nullptr; S* fpx = nullptr;   // F
+  int64_t* fhp = nullptr; int* fhi = nullptr; S* fhx = nullptr;   // F^H
+  int64_t nnz_f = 0;
+  std::vector<int> fp_lanes, fh_lanes;       // lanes per row of each level's F and F^H rows
+  std::vector<int64_t> fh_row0;              // first row pointer of each level's F^H block in fhp
+  void *cy = nullptr, *cyb = nullptr, *ct = nullptr;
 };
 
 namespace k {
@@ -118,6 +135,8 @@ template <class T, class S> void ildl_apply(const DevFactor<S>& F, bool spd, con
 // the same through the captured graph (builds it on first use); F.rhs_in and
 // F.sol_out must hold n entries of T
 template <class T, class S> void ildl_apply_graph(DevFactor<S>& F, bool spd, const T* b, T* x, cudaStream_t s);
+// lanes of a warp that share one row of a given mean length in the row kernels
+int lanes_per_row(double entries_per_row);
 // split the level lists of F into wide levels and runs of narrow levels
 template <class S> void ildl_plan(DevFactor<S>& F, const std::vector<int64_t>& lp_host, const std::vector<int64_t>& up_host,
                                   const std::vector<int>& brows_host);

@@ -93,16 +93,25 @@ template <class S> struct Copies {
   double sigma = 0, tol = 0, shift = 0, droptol = 0, mem = 0, gap = 0;
   int neig_in = 0, lx = 0, n = 0;
   long nnz_a = 0, nnz_b = 0;
+  bool diag_only = false;  // JA(1) < 0: A (and B) hold the N diagonal values, IA/IB/JB unreferenced
   int ijob = 0, ndx1 = 0, ndx2 = 0, ndx3 = 0;  // the request last handed to the caller
 
-  void load(int N, const S* A, const int* IA, const S* B, const int* IB, const float* EIGS, const float* RES,
-            const S* X, int LX, int NEIG, const float* SIGMA, const float* TOL, const float* SHIFT,
-            const float* DROPTOL, const float* MEM, const float* GAP) {
+  void load(int N, const S* A, const int* JA, const int* IA, const S* B, const int* IB, const float* EIGS,
+            const float* RES, const S* X, int LX, int NEIG, const float* SIGMA, const float* TOL,
+            const float* SHIFT, const float* DROPTOL, const float* MEM, const float* GAP) {
     n = N;
     lx = LX;
     neig_in = NEIG;
-    nnz_a = A ? (long)IA[N] - IA[0] : 0;
-    nnz_b = B ? (long)IB[N] - IB[0] : 0;
+    // diagonal preconditioning (PJD.F:309-317, 626-634): the reference reads
+    // A(1..N) (and B(1..N)) only and leaves A, JA, IA, B, JB, IB unchanged
+    diag_only = A && JA && JA[0] < 0;
+    if (diag_only) {
+      nnz_a = N;
+      nnz_b = B ? N : 0;
+    } else {
+      nnz_a = A ? (long)IA[N] - IA[0] : 0;
+      nnz_b = B ? (long)IB[N] - IB[0] : 0;
+    }
     a.resize(nnz_a);
     if (A) widen(A, a.data(), nnz_a);
     b.resize(nnz_b);
@@ -124,8 +133,8 @@ template <class S> struct Copies {
   }
   // everything the double driver may have written, rounded into the caller's arrays
   void store(S* A, S* B, float* EIGS, float* RES, S* X, float* SHIFT, float* DROPTOL, float* MEM, float* GAP) {
-    if (A) narrow(a.data(), A, nnz_a);
-    if (B) narrow(b.data(), B, nnz_b);
+    if (A && !diag_only) narrow(a.data(), A, nnz_a);
+    if (B && !diag_only) narrow(b.data(), B, nnz_b);
     narrow(x.data(), X, (long)x.size());
     narrow(eigs.data(), EIGS, (long)eigs.size());
     narrow(res.data(), RES, (long)res.size());
@@ -175,7 +184,7 @@ JDG_SAPI void JDG_S(spjd_)(int* N, float* A, int* JA, int* IA, float* EIGS, floa
                    float* DROPTOL, float* MEM, int* ICNTL, int* IPRINT, int* INFO, float* GAP) {
   guarded(INFO, [&] {
     Copies<float> c;
-    c.load(*N, A, IA, nullptr, nullptr, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, SHIFT, DROPTOL, MEM, GAP);
+    c.load(*N, A, JA, IA, nullptr, nullptr, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, SHIFT, DROPTOL, MEM, GAP);
     JDG_S(dpjd_)(N, c.a.data(), JA, IA, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma, ISEARCH, NINIT, MADSPACE,
           ITER, &c.tol, &c.shift, &c.droptol, &c.mem, ICNTL, IPRINT, INFO, &c.gap);
     c.store(A, nullptr, EIGS, RES, X, SHIFT, DROPTOL, MEM, GAP);
@@ -188,7 +197,7 @@ JDG_SAPI void JDG_S(spjd_gep_)(int* N, float* A, int* JA, int* IA, float* B, int
                        float* GAP) {
   guarded(INFO, [&] {
     Copies<float> c;
-    c.load(*N, A, IA, B, IB, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, SHIFT, DROPTOL, MEM, GAP);
+    c.load(*N, A, JA, IA, B, IB, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, SHIFT, DROPTOL, MEM, GAP);
     JDG_S(dpjd_gep_)(N, c.a.data(), JA, IA, c.b.data(), JB, IB, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma,
               ISEARCH, NINIT, MADSPACE, ITER, &c.tol, &c.shift, &c.droptol, &c.mem, ICNTL, IPRINT, INFO, &c.gap);
     c.store(A, B, EIGS, RES, X, SHIFT, DROPTOL, MEM, GAP);
@@ -201,7 +210,7 @@ JDG_SAPI void JDG_S(spjdrevcom_)(int* N, float* A, int* JA, int* IA, float* EIGS
                          int* INFO, float* GAP) {
   guarded(INFO, [&] {
     Copies<float>& c = revcom_copies<float>(0);
-    if (*IJOB == 0) c.load(*N, A, IA, nullptr, nullptr, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, SHIFT, DROPTOL, MEM, GAP);
+    if (*IJOB == 0) c.load(*N, A, JA, IA, nullptr, nullptr, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, SHIFT, DROPTOL, MEM, GAP);
     else c.take_back(X, false);
     JDG_S(dpjdrevcom_)(N, c.a.data(), JA, IA, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma, ISEARCH, NINIT,
                 MADSPACE, ITER, &c.tol, &c.shift, &c.droptol, &c.mem, ICNTL, IJOB, NDX1, NDX2, IPRINT, INFO, &c.gap);
@@ -222,7 +231,7 @@ JDG_SAPI void JDG_S(spjdrevcom_gep_)(int* N, float* A, int* JA, int* IA, float* 
                              int* NDX1, int* NDX2, int* NDX3, int* IPRINT, int* INFO, float* GAP) {
   guarded(INFO, [&] {
     Copies<float>& c = revcom_copies<float>(0);
-    if (*IJOB == 0) c.load(*N, A, IA, B, IB, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, SHIFT, DROPTOL, MEM, GAP);
+    if (*IJOB == 0) c.load(*N, A, JA, IA, B, IB, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, SHIFT, DROPTOL, MEM, GAP);
     else c.take_back(X, true);
     JDG_S(dpjdrevcom_gep_)(N, c.a.data(), JA, IA, c.b.data(), JB, IB, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG,
                     &c.sigma, ISEARCH, NINIT, MADSPACE, ITER, &c.tol, &c.shift, &c.droptol, &c.mem, ICNTL, IJOB, NDX1,
@@ -245,7 +254,7 @@ JDG_SAPI void JDG_S(sjdrevcom_)(int* N, float* EIGS, float* RES, float* X, int* 
   guarded(INFO, [&] {
     Copies<float>& c = revcom_copies<float>(1);
     if (*IJOB == 0)
-      c.load(*N, nullptr, nullptr, nullptr, nullptr, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, nullptr, nullptr, nullptr, GAP);
+      c.load(*N, nullptr, nullptr, nullptr, nullptr, nullptr, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, nullptr, nullptr, nullptr, GAP);
     else c.take_back(X, false);
     JDG_S(djdrevcom_)(N, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma, ISEARCH, NINIT, MADSPACE, ITER, &c.tol,
                IJOB, NDX1, NDX2, IPRINT, INFO, &c.gap);
@@ -266,7 +275,7 @@ JDG_SAPI void JDG_S(sjdrevcom_gep_)(int* N, float* EIGS, float* RES, float* X, i
   guarded(INFO, [&] {
     Copies<float>& c = revcom_copies<float>(1);
     if (*IJOB == 0)
-      c.load(*N, nullptr, nullptr, nullptr, nullptr, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, nullptr, nullptr, nullptr, GAP);
+      c.load(*N, nullptr, nullptr, nullptr, nullptr, nullptr, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, nullptr, nullptr, nullptr, GAP);
     else c.take_back(X, true);
     JDG_S(djdrevcom_gep_)(N, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma, ISEARCH, NINIT, MADSPACE, ITER,
                    &c.tol, IJOB, NDX1, NDX2, NDX3, IPRINT, INFO, &c.gap);
@@ -294,7 +303,7 @@ JDG_SAPI void JDG_S(cpjd_)(int* N, jdg_ccomplex* A, int* JA, int* IA, float* EIG
                    float* SHIFT, float* DROPTOL, float* MEM, int* ICNTL, int* IPRINT, int* INFO, float* GAP) {
   guarded(INFO, [&] {
     Copies<cf> c;
-    c.load(*N, A, IA, nullptr, nullptr, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, SHIFT, DROPTOL, MEM, GAP);
+    c.load(*N, A, JA, IA, nullptr, nullptr, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, SHIFT, DROPTOL, MEM, GAP);
     JDG_S(zpjd_)(N, c.a.data(), JA, IA, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma, ISEARCH, NINIT, MADSPACE,
           ITER, &c.tol, &c.shift, &c.droptol, &c.mem, ICNTL, IPRINT, INFO, &c.gap);
     c.store(A, nullptr, EIGS, RES, X, SHIFT, DROPTOL, MEM, GAP);
@@ -307,7 +316,7 @@ JDG_SAPI void JDG_S(cpjd_gep_)(int* N, jdg_ccomplex* A, int* JA, int* IA, jdg_cc
                        int* IPRINT, int* INFO, float* GAP) {
   guarded(INFO, [&] {
     Copies<cf> c;
-    c.load(*N, A, IA, B, IB, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, SHIFT, DROPTOL, MEM, GAP);
+    c.load(*N, A, JA, IA, B, IB, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, SHIFT, DROPTOL, MEM, GAP);
     JDG_S(zpjd_gep_)(N, c.a.data(), JA, IA, c.b.data(), JB, IB, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma,
               ISEARCH, NINIT, MADSPACE, ITER, &c.tol, &c.shift, &c.droptol, &c.mem, ICNTL, IPRINT, INFO, &c.gap);
     c.store(A, B, EIGS, RES, X, SHIFT, DROPTOL, MEM, GAP);
@@ -320,7 +329,7 @@ JDG_SAPI void JDG_S(cpjdrevcom_)(int* N, jdg_ccomplex* A, int* JA, int* IA, floa
                          int* IPRINT, int* INFO, float* GAP) {
   guarded(INFO, [&] {
     Copies<cf>& c = revcom_copies<cf>(0);
-    if (*IJOB == 0) c.load(*N, A, IA, nullptr, nullptr, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, SHIFT, DROPTOL, MEM, GAP);
+    if (*IJOB == 0) c.load(*N, A, JA, IA, nullptr, nullptr, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, SHIFT, DROPTOL, MEM, GAP);
     else c.take_back(X, false);
     JDG_S(zpjdrevcom_)(N, c.a.data(), JA, IA, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma, ISEARCH, NINIT,
                 MADSPACE, ITER, &c.tol, &c.shift, &c.droptol, &c.mem, ICNTL, IJOB, NDX1, NDX2, IPRINT, INFO, &c.gap);
@@ -342,7 +351,7 @@ JDG_SAPI void JDG_S(cpjdrevcom_gep_)(int* N, jdg_ccomplex* A, int* JA, int* IA, 
                              int* INFO, float* GAP) {
   guarded(INFO, [&] {
     Copies<cf>& c = revcom_copies<cf>(0);
-    if (*IJOB == 0) c.load(*N, A, IA, B, IB, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, SHIFT, DROPTOL, MEM, GAP);
+    if (*IJOB == 0) c.load(*N, A, JA, IA, B, IB, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, SHIFT, DROPTOL, MEM, GAP);
     else c.take_back(X, true);
     JDG_S(zpjdrevcom_gep_)(N, c.a.data(), JA, IA, c.b.data(), JB, IB, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG,
                     &c.sigma, ISEARCH, NINIT, MADSPACE, ITER, &c.tol, &c.shift, &c.droptol, &c.mem, ICNTL, IJOB, NDX1,
@@ -365,7 +374,7 @@ JDG_SAPI void JDG_S(cjdrevcom_)(int* N, float* EIGS, float* RES, jdg_ccomplex* X
   guarded(INFO, [&] {
     Copies<cf>& c = revcom_copies<cf>(1);
     if (*IJOB == 0)
-      c.load(*N, nullptr, nullptr, nullptr, nullptr, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, nullptr, nullptr, nullptr, GAP);
+      c.load(*N, nullptr, nullptr, nullptr, nullptr, nullptr, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, nullptr, nullptr, nullptr, GAP);
     else c.take_back(X, false);
     JDG_S(zjdrevcom_)(N, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma, ISEARCH, NINIT, MADSPACE, ITER, &c.tol,
                IJOB, NDX1, NDX2, IPRINT, INFO, &c.gap);
@@ -386,7 +395,7 @@ JDG_SAPI void JDG_S(cjdrevcom_gep_)(int* N, float* EIGS, float* RES, jdg_ccomple
   guarded(INFO, [&] {
     Copies<cf>& c = revcom_copies<cf>(1);
     if (*IJOB == 0)
-      c.load(*N, nullptr, nullptr, nullptr, nullptr, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, nullptr, nullptr, nullptr, GAP);
+      c.load(*N, nullptr, nullptr, nullptr, nullptr, nullptr, EIGS, RES, X, *LX, *NEIG, SIGMA, TOL, nullptr, nullptr, nullptr, GAP);
     else c.take_back(X, true);
     JDG_S(zjdrevcom_gep_)(N, c.eigs.data(), c.res.data(), c.x.data(), LX, NEIG, &c.sigma, ISEARCH, NINIT, MADSPACE, ITER,
                    &c.tol, IJOB, NDX1, NDX2, NDX3, IPRINT, INFO, &c.gap);

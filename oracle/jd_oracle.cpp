@@ -1,3 +1,4 @@
+#include <cstdlib>
 // Test infrastructure only: the CPU oracle of the JADAMILU drop-in.
 //
 // Restates, on the CPU and in plain loops, the reference's driver layer:
@@ -34,6 +35,24 @@ namespace orc {
 static double g_depth_weight = 64.0;
 static double g_drop_schur = -1.0;  // IldlcParams::droptol_schur (negative: its default rule)
 static int g_matching = 0;          // IldlcParams::matching
+// factor form for matrices of at least g_coupled_min_n rows (the library's
+// defaults: coupling blocks, Schur-contribution drop rule, look-ahead pivot
+// deferral, exact last level once a level's matrix is a third full); smaller
+// ones keep IldlcParams' own
+static int g_drop_rule = 1;         // IldlcParams::drop_rule
+static int g_coupling = 1;          // IldlcParams::coupling
+static double g_last_droptol = 0;   // IldlcParams::last_droptol
+static double g_last_fill = 1.0 / 3.0;  // IldlcParams::last_fill
+static int g_coupled_min_n = 20000;
+static int g_lookahead = 1;         // IldlcParams::lookahead
+static void factor_form(jdg::IldlcParams& p, int n) {
+  if (n < g_coupled_min_n) return;
+  p.lookahead = g_lookahead;
+  p.coupling = g_coupling;
+  p.drop_rule = g_drop_rule;
+  p.last_droptol = g_last_droptol;
+  p.last_fill = g_last_fill;
+}
 static int g_dense_min_rows = -1;   // IldlcParams::dense_min_rows (negative: its default)
 
 static double now_s() {
@@ -55,9 +74,77 @@ template <class T> void matveca(int n, const int* ia, const int* ja, const T* a,
   }
 }
 
+// Solve with one level's block B_l = L_l D_l L_l^H (|D_l| when spd) in place
+// on v[a, e): the level's rows of L reference only columns in [a, e).
+template <class T, class S>
+void level_bsolve(const jdg::IldlcFactor<T>& F, bool spd, int a, int e, std::vector<S>& v) {
+  for (int p = a; p < e; ++p) {
+    S s = v[p];
+    for (int64_t q = F.lp[p]; q < F.lp[p + 1]; ++q) s -= S(F.lx[q]) * v[F.li[q]];
+    v[p] = s;
+  }
+  const std::vector<T>& di = spd ? F.ainv : F.dinv;
+  const std::vector<T>& dof = spd ? F.aoff : F.doff;
+  for (int p = a; p < e; ++p) {
+    if (F.blk[p] == 1) {
+      v[p] = S(di[p]) * v[p];
+    } else if (F.blk[p] == 2) {
+      S a0 = v[p], a1 = v[p + 1];
+      S o = S(dof[p]);
+      v[p] = S(di[p]) * a0 + o * a1;
+      v[p + 1] = cj(o) * a0 + S(di[p + 1]) * a1;
+      ++p;
+    }
+  }
+  for (int p = e - 1; p >= a; --p) {
+    S w = v[p];
+    for (int64_t q = F.lp[p]; q < F.lp[p + 1]; ++q) v[F.li[q]] -= cj(S(F.lx[q])) * w;
+  }
+}
+
+// Multilevel application with the coupling blocks (the block solve of
+// symAMGsol.c:173-330): per level l, with the level's rows B and the later
+// rows C,
+//   forward:  y_B = B^{-1} b_B,  b_C -= F^H y_B   (then the next level on C),
+//   backward: x_B = y_B - B^{-1} (F x_C).
+// With spd every B^{-1} uses |D|, which keeps the operator Hermitian positive
+// definite: it is P^H diag(|B|^{-1}, |S|^{-1}) P with P = [I 0; -F^H |B|^{-1} I].
+template <class T, class S>
+void ildl_apply_coupled(const jdg::IldlcFactor<T>& F, bool spd, const T* b, T* x, std::vector<S>& y) {
+  const int n = F.n;
+  const int nlev = (int)F.level_start.size() - 1;
+  y.resize(n);
+  std::vector<S> yb(n), t(n);
+  for (int p = 0; p < n; ++p) y[p] = S(b[F.perm[p]]);
+  for (int l = 0; l < nlev; ++l) {
+    const int a = F.level_start[l], e = F.level_start[l + 1];
+    level_bsolve(F, spd, a, e, y);
+    if (l == nlev - 1) break;
+    for (int p = a; p < e; ++p) {
+      yb[p] = y[p];
+      for (int64_t q = F.fp[p]; q < F.fp[p + 1]; ++q) y[F.fi[q]] -= cj(S(F.fx[q])) * y[p];
+    }
+  }
+  for (int l = nlev - 2; l >= 0; --l) {
+    const int a = F.level_start[l], e = F.level_start[l + 1];
+    for (int p = a; p < e; ++p) {
+      S s = S(0);
+      for (int64_t q = F.fp[p]; q < F.fp[p + 1]; ++q) s += S(F.fx[q]) * y[F.fi[q]];
+      t[p] = s;
+    }
+    level_bsolve(F, spd, a, e, t);
+    for (int p = a; p < e; ++p) y[p] = yb[p] - t[p];
+  }
+  for (int p = 0; p < n; ++p) x[F.perm[p]] = T(y[p]);
+}
+
 // Application of the factor: x = P (L D L^H)^{-1} P^T b, with |D| when spd.
 template <class T, class S>
 void ildl_apply(const jdg::IldlcFactor<T>& F, bool spd, const T* b, T* x, std::vector<S>& y) {
+  if (F.coupling == 1) {
+    ildl_apply_coupled(F, spd, b, x, y);
+    return;
+  }
   const int n = F.n;
   y.resize(n);
   for (int p = 0; p < n; ++p) y[p] = S(b[F.perm[p]]);
@@ -269,6 +356,8 @@ int pjdinit(Global<T>& g, int n, T* a, int* ja, int* ia, const T* b, const int* 
     prm.depth_weight = g_depth_weight;
     prm.droptol_schur = g_drop_schur;
     prm.matching = g_matching;
+    factor_form(prm, n);
+    prm.verbose = std::getenv("JDG_FACTOR_VERBOSE") ? 1 : 0;
     if (g_dense_min_rows >= 0) prm.dense_min_rows = g_dense_min_rows;
     prm.droptol = DROPTOL;
     prm.condest = condest;
@@ -632,6 +721,18 @@ void orc_dimport_factor(int n, const int* perm, const long long* lp, const int* 
   g.factspd = 0;
   g.memused = g.memrequested = 1e30;
 }
+// the level structure and coupling blocks of an imported factor (after orc_dimport_factor)
+void orc_dimport_levels(int coupling, int nlev, const int* level_start, const long long* fp, const int* fi,
+                        const double* fx) {
+  auto& F = orc::G<double>().F;
+  F.level_start.assign(level_start, level_start + nlev + 1);
+  F.coupling = coupling;
+  if (coupling == 1) {
+    F.fp.assign(fp, fp + F.n + 1);
+    F.fi.assign(fi, fi + fp[F.n]);
+    F.fx.assign(fx, fx + fp[F.n]);
+  }
+}
 void orc_zpjdcleanup(void) { orc::G<cplx>().cleanup1(); }
 int orc_nfactor_d(void) { return orc::G<double>().nfactor; }
 
@@ -649,6 +750,14 @@ struct OrcFactorD { jdg::IldlcFactor<double> F; };
 void orc_set_depth_weight(double w) { orc::g_depth_weight = w; }
 void orc_set_drop_schur(double v) { orc::g_drop_schur = v; }
 void orc_set_matching(int v) { orc::g_matching = v; }
+void orc_set_drop_rule(int v) { orc::g_drop_rule = v; }
+void orc_set_coupling(int v) { orc::g_coupling = v; }
+void orc_set_last_level(double droptol, double fill) {
+  orc::g_last_droptol = droptol;
+  orc::g_last_fill = fill;
+}
+void orc_set_coupled_min_n(int v) { orc::g_coupled_min_n = v; }
+void orc_set_lookahead(int v) { orc::g_lookahead = v; }
 // The dense-block inverse tiles (project code under test): L is unit lower
 // triangular of order m given by rows rp/ci/cv (strictly lower, local
 // columns).  Writes nt*(nt+1)/2 tiles of 64x64 doubles each into tf and tb;
@@ -729,6 +838,8 @@ void* orc_dfactor(int n, const int* ia, const int* ja, const double* a, double s
   p.depth_weight = orc::g_depth_weight;
   p.droptol_schur = orc::g_drop_schur;
   p.matching = orc::g_matching;
+  orc::factor_form(p, n);
+  p.verbose = std::getenv("JDG_FACTOR_VERBOSE") ? 1 : 0;
   if (orc::g_dense_min_rows >= 0) p.dense_min_rows = orc::g_dense_min_rows;
   p.threads = g_threads;
   p.droptol = droptol;
@@ -750,6 +861,7 @@ void orc_dfactor_info(void* h, long* out) {
   long n2 = 0;
   for (int p = 0; p < F.n; ++p) n2 += F.blk[p] == 2;
   out[6] = n2;
+  out[7] = (long)F.fi.size();
 }
 // per elimination step: forward level; level_start boundaries into ls (size nlevels+1)
 void orc_dfactor_levels(void* h, int* flev, int* ls) {

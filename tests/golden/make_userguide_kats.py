@@ -6,7 +6,7 @@ norms and MATVEC counts).  This script reads that PostScript as text, takes
 the numbers between the known line anchors and writes userguide_kats.json.
 Run it once where the reference is available:
 
-    python tests/golden/make_userguide_kats.py /root/reference
+    python tests/golden/make_userguide_kats.py <JADAMILU source tree>
 """
 import json
 import os
@@ -55,4 +55,6 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_userguide_kats.py <path of the JADAMILU source tree>")
+    main(sys.argv[1])

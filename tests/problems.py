@@ -24,3 +24,12 @@ def dense_eigs(As, k, sigma=None):
         return w[:k]
     idx = np.argsort(np.abs(w - sigma), kind="stable")[:k]
     return np.sort(w[idx])
+
+
+def shift_invert_eigs(As, k, sigma=0.0):
+    """The k eigenvalues closest to sigma by shift-and-invert Lanczos (scipy's
+    ARPACK on a sparse LU of As - sigma I): an independent check for matrices
+    too large for a dense eigensolver."""
+    import scipy.sparse.linalg as sla
+    w = sla.eigsh(As.tocsc(), k=k, sigma=sigma, which="LM", tol=1e-13, return_eigenvectors=False)
+    return np.sort(w)

@@ -91,3 +91,65 @@ def test_memory_limit_reports_error(oracle):
     ia, ja, a = M.anderson3d(8, seed=3)
     F = oracle.Factor(ia, ja, a, shift=0.0, droptol=0.0, mem=1.5)
     assert F.ierr == -3
+
+
+class _CoupledForm:
+    """The coupling-block form on small matrices (the library uses it from
+    20000 rows on): every level keeps its own L and D, the coupling blocks F
+    are the level's matrix entries, the last level is exact once a third full."""
+
+    def __init__(self, oracle):
+        import ctypes as C
+        self.lib = oracle.lib()
+        self.lib.orc_set_coupled_min_n.argtypes = [C.c_int]
+
+    def __enter__(self):
+        self.lib.orc_set_coupled_min_n(0)
+        return self
+
+    def __exit__(self, *exc):
+        self.lib.orc_set_coupled_min_n(20000)
+
+
+@pytest.mark.parametrize("name", ["laplace6", "anderson7", "random_indefinite", "tridiag_zero_diag"])
+def test_coupled_form_exact_when_nothing_is_dropped(oracle, name):
+    ia, ja, a = CASES[name]()
+    A = M.to_scipy_full(ia, ja, a)
+    with _CoupledForm(oracle):
+        F = oracle.Factor(ia, ja, a, shift=0.1, droptol=0.0, mem=0)
+    assert F.ierr == 0
+    b = np.random.default_rng(1).standard_normal(A.shape[0])
+    x = F.apply(b)
+    As = A - 0.1 * sp.eye(A.shape[0])
+    assert np.linalg.norm(As @ x - b) <= 1e-9 * np.linalg.norm(b) * max(1, np.abs(As).max())
+
+
+def test_coupled_form_levels_and_spd(oracle):
+    """Deferred rows form levels; L has no entry across levels; the |D| form
+    is Hermitian positive definite."""
+    import ctypes as C
+    ia, ja, a = M.anderson3d(7, seed=4)
+    with _CoupledForm(oracle):
+        F = oracle.Factor(ia, ja, a, shift=0.0, droptol=3e-3, mem=0)
+    info = F.info()
+    assert info["nlevels"] >= 2
+    n = F.n
+    L = oracle.lib()
+    sizes = np.zeros(4, np.int64)
+    L.orc_dfactor_schedule.argtypes = [C.c_void_p] * 8
+    L.orc_dfactor_schedule(F.h, sizes.ctypes.data, None, None, None, None, None, None)
+    nf, nb = int(sizes[0]), int(sizes[1])
+    bufs = [np.zeros(nf + 1, np.int32), np.zeros(n, np.int32), np.zeros(nb + 1, np.int32), np.zeros(n, np.int32),
+            np.zeros(n + 1, np.int64), np.zeros(int(sizes[3]), np.int32)]
+    L.orc_dfactor_schedule(F.h, sizes.ctypes.data, *[v.ctypes.data for v in bufs])
+    lp, li = bufs[4], bufs[5]
+    flev = np.zeros(n, np.int32)
+    ls = np.zeros(info["nlevels"] + 1, np.int32)
+    L.orc_dfactor_levels.argtypes = [C.c_void_p] * 3
+    L.orc_dfactor_levels(F.h, flev.ctypes.data, ls.ctypes.data)
+    level_of = np.searchsorted(ls, np.arange(n), side="right") - 1
+    rows = np.repeat(np.arange(n), np.diff(lp))
+    assert np.array_equal(level_of[rows], level_of[li])
+    Mi = np.stack([F.apply(e, spd=True) for e in np.eye(n)], 1)
+    np.testing.assert_allclose(Mi, Mi.T, atol=1e-10 * np.abs(Mi).max())
+    assert np.linalg.eigvalsh(0.5 * (Mi + Mi.T)).min() > 0

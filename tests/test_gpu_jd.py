@@ -226,3 +226,22 @@ def test_generalized_harmonic_complex(gpu):
                      droptol=1e-3)
     assert r["info"] == 0 and r["neig"] == 4
     np.testing.assert_allclose(np.sort(r["eigs"]), ref, rtol=1e-9, atol=1e-12)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_anderson_coupled_form(gpu, oracle, precision):
+    """Anderson 28^3 (n = 21952): from 20000 rows the factor keeps each
+    level's L apart and couples the levels through F blocks.  Ten interior
+    eigenvalues against shift-and-invert Lanczos and the oracle (same factor
+    form), residuals at TOL."""
+    from problems import shift_invert_eigs
+    ia, ja, a = M.anderson3d(28, seed=0)
+    kw = dict(isearch=2, sigma=0.0, madspace=25, maxit=20000, tol=1e-10, droptol=3e-3, mem=60.0,
+              icntl=(0, 1, 0, 0, precision))
+    r = gpu.dpjd((a, ja, ia), 10, **kw)
+    assert r["info"] == 0 and r["neig"] == 10
+    As = M.to_scipy_full(ia, ja, a)
+    _close(r["eigs"], shift_invert_eigs(As, 10))
+    assert np.all(r["res"] <= 1.1e-10)
+    ro = oracle.dpjd(ia, ja, a, 10, **kw)
+    _close(r["eigs"], ro["eigs"])

@@ -91,3 +91,26 @@ def test_ildl_apply_tail_variants_match_oracle(gpu, oracle, variant, precision, 
             e32 = np.linalg.norm(F.apply(B[r], single=True) - xo) / np.linalg.norm(xo)
             tol = max(tol, 4 * e32)
         assert err <= tol, err
+
+
+@pytest.mark.parametrize("spd", [False, True])
+@pytest.mark.parametrize("precision,tol", [(0, 1e-11), (1, 2e-5)])
+def test_ildl_apply_coupled_matches_oracle(gpu, oracle, spd, precision, tol):
+    """From 20000 rows on the factor keeps each level's L and D apart with
+    coupling blocks F (the multilevel form of symAMGsol.c:173-330): Anderson
+    28^3 (n = 21952), applied on the GPU as per-level sub-factors, F and F^H,
+    against the oracle's application of the same factor."""
+    ia, ja, a = M.anderson3d(28, seed=2)
+    n = len(ia) - 1
+    F = oracle.Factor(ia, ja, a, shift=0.0, droptol=3e-3, mem=0)
+    assert F.ierr == 0 and F.info()["nlevels"] >= 2
+    B = np.random.default_rng(5).standard_normal((2, n))
+    Xg, info = gpu.ildl_apply((a, ja, ia), B, shift=0.0, droptol=3e-3, spd=spd, precision=precision)
+    assert info["nnz_l"] == F.info()["nnz_l"]
+    for r in range(2):
+        xo = F.apply(B[r], spd=spd)
+        err = np.linalg.norm(Xg[r] - xo) / np.linalg.norm(xo)
+        if precision == 1:
+            e32 = np.linalg.norm(F.apply(B[r], spd=spd, single=True) - xo) / np.linalg.norm(xo)
+            tol = max(tol, 4 * e32)
+        assert err <= tol, err

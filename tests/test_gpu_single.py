@@ -133,3 +133,56 @@ def test_sjdrevcom_single_precision_operators(gpu):
     w = np.linalg.eigvalsh(As.toarray().astype(np.float64))
     for lam in EIGS:
         assert np.min(np.abs(w - lam)) <= 1e-4 * max(1.0, abs(lam))
+
+
+def _spjdrevcom_diag(L, name, n, d, As, neig, rdt, kw):
+    """SPJDREVCOM / DPJDREVCOM with JA(1) < 0: A holds the N diagonal values,
+    JA and IA have one element each.  The user matvec runs in float32 for
+    both: DPJDREVCOM's request vectors are rounded to float32 first, as the
+    single-precision driver hands them out."""
+    mad = kw["madspace"]
+    lx = _lx(n, neig, mad)
+    A = np.array(d, rdt)
+    JA, IA = np.array([-1], np.int32), np.array([-7], np.int32)  # IA must not be read
+    X = np.zeros(lx, rdt)
+    EIGS, RES, GAP = np.zeros(neig, rdt), np.zeros(neig, rdt), np.zeros(1, rdt)
+    sc = {k: np.array([kw[k]], rdt) for k in ("sigma", "tol", "shift", "droptol", "mem")}
+    N, LX, NEIG, ISEARCH, NINIT, MAD, ITER = (_i(v) for v in (n, lx, neig, kw["isearch"], 0, mad, kw["maxit"]))
+    ICNTL, IJOB, NDX1, NDX2, IPRINT, INFO = np.zeros(5, np.int32), _i(0), _i(0), _i(0), _i(0), _i(0)
+    f = getattr(L, name)
+    f.argtypes = [P] * 25
+    Am = As.astype(np.float32)
+    while True:
+        f(_p(N), _p(A), _p(JA), _p(IA), _p(EIGS), _p(RES), _p(X), _p(LX), _p(NEIG), _p(sc["sigma"]), _p(ISEARCH),
+          _p(NINIT), _p(MAD), _p(ITER), _p(sc["tol"]), _p(sc["shift"]), _p(sc["droptol"]), _p(sc["mem"]), _p(ICNTL),
+          _p(IJOB), _p(NDX1), _p(NDX2), _p(IPRINT), _p(INFO), _p(GAP))
+        if IJOB[0] == 0:
+            break
+        assert IJOB[0] == 1
+        i1, i2 = int(NDX1[0]) - 1, int(NDX2[0]) - 1
+        X[i2:i2 + n] = Am @ X[i1:i1 + n].astype(np.float32)
+    k = int(NEIG[0])
+    return int(INFO[0]), EIGS[:k].copy(), int(ITER[0]), A, JA, IA
+
+
+def test_spjdrevcom_diagonal_preconditioning(gpu):
+    """JA(1) < 0 (PJD.F:309-317): the single-precision revcom driver reads only
+    A(1..N), never IA, leaves A/JA/IA unchanged, and returns the rounded
+    results of DPJDREVCOM on the same rounded data."""
+    L = gpu.load()
+    ia, ja, a = M.anderson3d(8, seed=7)
+    n = len(ia) - 1
+    As = M.to_scipy_full(ia, ja, np.asarray(a, np.float32).astype(np.float64)).tocsr()
+    d32 = As.diagonal().astype(np.float32)
+    kw = dict(KW, isearch=0, maxit=20000)
+    kw32 = {k: (float(np.float32(v)) if isinstance(v, float) else v) for k, v in kw.items()}
+    info_s, eig_s, it_s, A_s, JA_s, IA_s = _spjdrevcom_diag(L, "spjdrevcom_", n, d32, As, 4, np.float32, kw32)
+    assert info_s == 0 and len(eig_s) == 4
+    assert np.array_equal(A_s, d32) and JA_s[0] == -1 and IA_s[0] == -7
+    info_d, eig_d, it_d, A_d, _, _ = _spjdrevcom_diag(L, "dpjdrevcom_", n, d32.astype(np.float64), As, 4, np.float64,
+                                                      kw32)
+    assert info_d == 0 and it_s == it_d
+    assert np.array_equal(eig_s, eig_d.astype(np.float32))
+    w = np.linalg.eigvalsh(As.toarray())
+    for lam in eig_s:
+        assert np.min(np.abs(w - lam)) <= 1e-4 * max(1.0, abs(lam))
