@@ -74,6 +74,10 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="budget of the CPU-baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
+    ap.add_argument("--no-precision-check", action="store_true",
+                    help="skip the float64 / bfloat16 comparison solves after the timed region")
+    ap.add_argument("--ref-seconds", type=float, default=180.0,
+                    help="reference arm: budget of all its steps (capped samples when complete solves do not fit)")
     args = ap.parse_args()
     defaults = {"anderson": (DEFAULT_SIZE, 1, 10), "laplace": (20, 0, 10), "tightbinding": (64, 1, 8),
                 "fem": (512, 0, 6), "batch": (40, 1, 5)}[args.workload]
@@ -320,6 +324,57 @@ def cpu_baseline_sample(J, ia, ja, a, args, gpu_iter, w=None):
                       f"({per_mv * 1e3:.1f} ms/MATVEC) scaled to the GPU solve's {gpu_iter} MATVECs"}
 
 
+def precision_check(J, w, args, timed, stream, torch):
+    """One solve with the factor in float64 (the plain FP64 GPU method) and
+    one in bfloat16, reusing the host factor (ICNTL(2) = -1, ICNTL(5) 0 / 2):
+    seconds per solve (CUDA events), MATVECs, and per eigenvalue the error of
+    the timed run's eigenvalues against the float64 run's."""
+    out = {}
+    ref = None
+    for name, prec in (("fp64", 0), ("bf16", 2)):
+        a2 = argparse.Namespace(**vars(args))
+        a2.precision = prec
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        r = run_solve(J, w, a2, -1)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ok = r["info"] == 0 and r["neig"] == args.neig
+        ev = np.sort(r["eigs"])
+        out[name] = {"s_per_solve": e0.elapsed_time(e1) / 1e3, "matvec": r["iter"], "converged": ok,
+                     "max_res": float(np.max(r["res"])) if len(r["res"]) else None}
+        if prec == 0:
+            ref = ev if ok else None
+        elif ref is not None and ok:
+            out[name]["eig_rel_err_vs_fp64"] = (np.abs(ev - ref) / np.abs(ref)).tolist()
+    mixed = np.sort(timed["eigs"])
+    if ref is not None and len(mixed) == len(ref):
+        err = np.abs(mixed - ref)
+        out["mixed_eig_abs_err_vs_fp64"] = err.tolist()
+        out["mixed_eig_rel_err_vs_fp64"] = (err / np.abs(ref)).tolist()
+        out["mixed_max_rel_err_vs_fp64"] = float(np.max(err / np.abs(ref)))
+    # restore the timed run's factor precision for the legs that follow
+    run_solve(J, w, args, -1)
+    return out
+
+
+def profile_traffic(w, args):
+    """DRAM bytes (read + write) per preconditioner application from the
+    committed ncu summary of the same workload, when there is one."""
+    path = os.path.join(ROOT, "profiles", "ildl_apply_anderson%d.md" % args.size)
+    if w["name"] != "anderson" or not os.path.exists(path):
+        return None
+    key = "traffic_bytes_per_application_%s:" % {0: "fp64", 1: "fp32", 2: "bf16"}[args.precision]
+    for line in open(path):
+        if line.strip().startswith(key):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
 def run_gb300(args):
     rank, world, local = dist_env()
     import torch
@@ -382,7 +437,7 @@ def run_gb300(args):
     eigs = np.sort(results[-1]["eigs"])
     # roofline of the dominant kernels (preconditioner application) and of SpMV
     # (real standard problems: the resident matrix and the real factor)
-    pb = np.full(5, np.nan)
+    pb = np.full(6, np.nan)
     sb = np.full(4, np.nan)
     if w["resident"]:
         L.jdgpu_dprecond_bench.argtypes = [C.c_int, C.c_void_p]
@@ -390,8 +445,18 @@ def run_gb300(args):
         L.jdgpu_dspmv_bench.argtypes = [C.c_int, C.c_void_p]
         L.jdgpu_dspmv_bench(50, sb.ctypes.data_as(C.c_void_p))
     peak, peak_kind = measured_peaks()
-    prec_gbs = pb[1] / (pb[0] * 1e-3) / 1e9
+    # achieved bandwidth on the algorithmic bytes of one application (pb[5]:
+    # every L entry once per sweep, F and F^H, D, vectors); pb[1] adds what the
+    # dense blocks' explicit-inverse tiles stream instead of their L entries
+    prec_gbs = pb[5] / (pb[0] * 1e-3) / 1e9
+    prec_streamed_gbs = pb[1] / (pb[0] * 1e-3) / 1e9
     spmv_gbs = sb[1] / (sb[0] * 1e-3) / 1e9
+    # the same factor in float64 (the plain FP64 method) and in bfloat16, one
+    # build: seconds per solve and the error of each eigenvalue of the timed
+    # (mixed) run against the float64 run
+    prec_check = None
+    if w["resident"] and w["kind"] == "d" and not args.no_precision_check:
+        prec_check = precision_check(J, w, args, results[-1], stream, torch)
     # e2e: through the C ABI with host buffers (matrix upload + eigenvector download)
     if w["resident"]:
         J.release_matrix()
@@ -444,13 +509,16 @@ def run_gb300(args):
                        "info": [rr["info"] for rr in results], "neig": [rr["neig"] for rr in results],
                        "max_res": max(float(np.max(rr["res"])) if len(rr["res"]) else 0.0 for rr in results)},
             "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-            "roofline": {"kernel": f"ildl_apply graph (level sweeps + dense-block tile products, {inner})",
+            "roofline": {"kernel": f"ildl_apply graph (level sweeps, coupling blocks, dense-block tiles; {inner})",
                          "bound": "hbm",
                          "achieved": prec_gbs, "peak": peak, "unit": "GB/s", "frac": prec_gbs / peak,
-                         "traffic": None, "bytes_per_launch": pb[1], "ms_per_launch": pb[0],
-                         "peak_kind": peak_kind},
+                         "traffic": profile_traffic(w, args), "bytes_per_launch": pb[5], "ms_per_launch": pb[0],
+                         "kernels_per_launch": pb[4], "peak_kind": peak_kind,
+                         "streamed": {"bytes_per_launch": pb[1], "achieved": prec_streamed_gbs,
+                                      "frac": prec_streamed_gbs / peak}},
             "roofline_spmv": {"achieved": spmv_gbs, "peak": peak, "unit": "GB/s", "frac": spmv_gbs / peak,
                               "bytes_per_launch": sb[1], "ms_per_launch": sb[0]},
+            "precision_check": prec_check,
             "gpu_launches": int(launches),
             "clocks": clk,
             "cpu_baseline": cpu,
@@ -461,15 +529,33 @@ def run_gb300(args):
         dist.destroy_process_group()
 
 
+def fixture_matvecs(args):
+    """MATVECs of the oracle's complete solve of the Anderson workload of this
+    size, from the committed fixture (tests/golden/anderson_eigs.json), when
+    the settings match; None otherwise."""
+    path = os.path.join(ROOT, "tests", "golden", "anderson_eigs.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+    except Exception:
+        return None
+    st = d.get("settings", {})
+    if st.get("droptol") != args.droptol or list(st.get("icntl", []))[4:5] != [args.precision] or args.neig != 10:
+        return None
+    case = d.get("cases", {}).get(str(args.size))
+    return int(case["oracle_matvec"]) if case and "oracle_matvec" in case else None
+
+
 def run_reference(args):
     """The reference path on the host cores: the CPU oracle (the reference's
     algorithm restated; the Fortran library cannot be built on this image).
 
     The factor is computed once (all host threads) and every step is one
-    complete solve reusing it (ICNTL(2) = -1), as in the GPU arm.  Setting
-    JDG_MATVEC_PER_SOLVE replaces the complete solves by capped samples
-    scaled to that MATVEC count, for lattices too large to solve on one
-    core within minutes."""
+    complete solve reusing it (ICNTL(2) = -1), as in the GPU arm.  When a
+    complete solve does not fit the step budget (--ref-seconds over all
+    steps), each step runs the MATVECs that fit and is scaled to the MATVEC
+    count of the oracle's complete solve of the same workload, recorded in
+    tests/golden/anderson_eigs.json."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
@@ -497,12 +583,23 @@ def run_reference(args):
     kw["maxit"] = 4
     oracle_lib.dpjd(ia, ja, a, args.neig, **kw, **extra)
     factor_s = time.perf_counter() - t0
-    mv = int(os.environ.get("JDG_MATVEC_PER_SOLVE", "0")) or None
+    # Each step is a complete solve when one fits the step budget; otherwise a
+    # solve capped at the MATVECs that fit, scaled to the oracle's own MATVEC
+    # count of a complete solve of this workload (the committed fixture), so
+    # the whole arm ends within about --ref-seconds.
+    budget = args.ref_seconds / max(1, args.warmup + args.steps)
+    kw = solve_kwargs(args, -1, w)
+    kw["maxit"] = 16
+    t0 = time.perf_counter()
+    r = oracle_lib.dpjd(ia, ja, a, args.neig, **kw, **extra)
+    per_mv = (time.perf_counter() - t0) / max(1, r["iter"])
+    full = fixture_matvecs(args) if w["name"] == "anderson" else None
+    mv = full if (full is not None and per_mv * full > budget) else None
     times, iters, infos = [], [], []
     for step in range(args.warmup + args.steps):
         kw = solve_kwargs(args, -1, w)
         if mv:
-            kw["maxit"] = max(16, mv // 10)
+            kw["maxit"] = max(16, int(budget / per_mv))
         t0 = time.perf_counter()
         r = oracle_lib.dpjd(ia, ja, a, args.neig, **kw, **extra)
         dt = time.perf_counter() - t0
@@ -511,7 +608,7 @@ def run_reference(args):
             iters.append(r["iter"])
             infos.append(r["info"])
     v = float(np.median(times))
-    sample = (f"CPU oracle, {'capped samples scaled to %d MATVECs' % mv if mv else 'complete solves'}, "
+    sample = (f"CPU oracle, {'capped samples scaled to %d MATVECs (its complete solve)' % mv if mv else 'complete solves'}, "
               f"factor {factor_s:.1f} s on {threads} threads (untimed), solve on 1 core, "
               f"MATVECs {iters}, INFO {infos}")
     metric = METRIC if w["name"] == "anderson" else f"s to {args.neig} eigpairs at resid 1e-10 ({w['name']})"

@@ -107,3 +107,60 @@ def test_eigvec_loss_grad_matches_central_differences(gpu):
             f.append(loss(Kp))
         err = max(err, abs((f[0] - f[1]) / (2 * h) - grad[q]))
     assert err <= 1e-6 * np.abs(grad).max(), err
+
+
+def test_eig_grad_fem512_central_differences(gpu, oracle):
+    """The differentiation configuration at full size: P1-FEM K x = lambda M x
+    on 512 x 512 nodes (n = 260,100), gradient of the sum of the 6 smallest
+    eigenvalues with respect to every stored entry of K (jdgpu_deig_grad),
+    against central differences with step h = 1e-6 on 100 seeded entries.
+    Each difference re-solves K +- h E_q on the GPU (warm start from the
+    unperturbed eigenvectors, the kept preconditioner: ICNTL(2) = -1).
+
+    Bound: 1e-6 max|g| plus the rounding floor of a difference quotient,
+    16 eps sum|lambda| / h (the eigenvalue sums carry rounding of a few eps
+    |lambda| each).  For 3 of the entries the oracle (the reference's
+    algorithm on the CPU) solves the same perturbed pencils: its eigenvalues
+    agree with the GPU's to 1e-10 relative and its differences meet the same
+    bound."""
+    K, Mm = M.fem_p1(512, seed=3)
+    B = (Mm[2], Mm[1], Mm[0])
+    kw = dict(isearch=0, madspace=20, maxit=20000, tol=1e-10, droptol=1e-3)
+    r = gpu.dpjd_gep((K[2], K[1], K[0]), B, 6, icntl=(0, 1, 0, 0, 0), **kw)
+    assert r["info"] == 0 and r["neig"] == 6
+    a, ja, ia = r["a"], r["ja"], r["ia"]  # DPJD put each row's diagonal first
+    md = M.to_scipy_full(*Mm).diagonal()
+    order = np.argsort(r["eigs"])
+    X0 = r["x"][:, order].copy()
+    g = gpu.eig_grad((a, ja, ia), X0, bdiag=md)
+    h = 1e-6
+    floor = 16 * np.finfo(float).eps * np.sum(np.abs(r["eigs"])) / h
+    bound = 1e-6 * np.abs(g).max() + floor
+    qs = np.random.default_rng(11).choice(len(a), 100, replace=False)
+    sums = {}
+    worst = 0.0
+    for q in qs:
+        f = []
+        for sgn in (1.0, -1.0):
+            ap = a.copy()
+            ap[q] += sgn * h
+            rp = gpu.dpjd_gep((ap, ja, ia), B, 6, ninit=6, x=X0, icntl=(0, -1, 0, 0, 0), **kw)
+            assert rp["info"] == 0 and rp["neig"] == 6
+            f.append(np.sort(rp["eigs"]))
+        sums[int(q)] = f
+        worst = max(worst, abs((f[0].sum() - f[1].sum()) / (2 * h) - g[q]))
+    assert worst <= bound, (worst, bound)
+    # the oracle at the same perturbed inputs (its own kept factor of K)
+    ro = oracle.dpjd(ia, ja, a, 6, b=(Mm[0], Mm[1], Mm[2]), ninit=6, x=X0, icntl=(0, 1, 0, 0, 0), **kw)
+    assert ro["info"] == 0
+    for q in qs[:3]:
+        fo = []
+        for k, sgn in enumerate((1.0, -1.0)):
+            ap = a.copy()
+            ap[q] += sgn * h
+            rp = oracle.dpjd(ia, ja, ap, 6, b=(Mm[0], Mm[1], Mm[2]), ninit=6, x=X0, icntl=(0, -1, 0, 0, 0), **kw)
+            assert rp["info"] == 0 and rp["neig"] == 6
+            eo = np.sort(rp["eigs"])
+            np.testing.assert_allclose(eo, sums[int(q)][k], rtol=1e-10, atol=0)
+            fo.append(eo.sum())
+        assert abs((fo[0] - fo[1]) / (2 * h) - g[q]) <= bound
