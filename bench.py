@@ -47,7 +47,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "s to 10 eigpairs at resid 1e-10 (3D Anderson, sigma=0, FP32 factor / FP64 outer)"
-DEFAULT_SIZE = 40
+DEFAULT_SIZE = 100
 
 
 def parse():
@@ -66,8 +66,9 @@ def parse():
     ap.add_argument("--size", type=int, default=None,
                     help="lattice edge m (anderson: n = m^3, default %d, 100 is the named 1e6 case; laplace 20; "
                          "tightbinding 64; fem: nodes per side, 512)" % DEFAULT_SIZE)
-    ap.add_argument("--droptol", type=float, default=3e-3)
-    ap.add_argument("--mem", type=float, default=60.0)
+    ap.add_argument("--droptol", type=float, default=1e-3,
+                    help="ILDLC drop tolerance (1e-3 and MEM 15 as the reference's Anderson sample)")
+    ap.add_argument("--mem", type=float, default=15.0)
     ap.add_argument("--precision", type=int, default=None,
                     help="ICNTL(5): 0 fp64, 1 fp32, 2 bf16 factor (default: 1 for anderson and tightbinding, 0 else)")
     ap.add_argument("--neig", type=int, default=None, help="default: 10 (anderson, laplace), 8, 6")

@@ -122,6 +122,9 @@ __device__ __forceinline__ cc ld_arith_nc(const bc* p) {
   asm("ld.global.nc.L1::no_allocate.v2.b16 {%0, %1}, [%2];" : "=h"(x), "=h"(y) : "l"(p));
   return cc(__bfloat162float(__ushort_as_bfloat16(x)), __bfloat162float(__ushort_as_bfloat16(y)));
 }
+// a stored entry converted to the arithmetic type A
+template <class A, class S> __device__ __forceinline__ A lda(const S* p) { return cvt<A>(ld_arith(p)); }
+template <class A, class S> __device__ __forceinline__ A ldan(const S* p) { return cvt<A>(ld_arith_nc(p)); }
 __device__ __forceinline__ int ld_idx_nc(const int* p) {
   int r;
   asm("ld.global.nc.L1::no_allocate.s32 %0, [%1];" : "=r"(r) : "l"(p));

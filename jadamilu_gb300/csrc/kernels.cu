@@ -345,12 +345,12 @@ __global__ void ildl_dsolve_kernel(int n, const signed char* __restrict__ blk, c
   if (s >= n) return;
   signed char b = blk[s];
   if (b == 1) {
-    y[s] = ld_arith(dv + s) * y[s];
+    y[s] = lda<A>(dv + s) * y[s];
   } else if (b == 2) {
     int t = partner[s];
-    A a0 = y[s], a1 = y[t], o = ld_arith(dof + s);
-    y[s] = fma_(ld_arith(dv + s), a0, o * a1);
-    y[t] = fma_(cj(o), a0, ld_arith(dv + t) * a1);
+    A a0 = y[s], a1 = y[t], o = lda<A>(dof + s);
+    y[s] = fma_(lda<A>(dv + s), a0, o * a1);
+    y[t] = fma_(cj(o), a0, lda<A>(dv + t) * a1);
   }
 }
 // A run of narrow levels [l0, l1) in one CTA: a warp per row, levels
@@ -385,7 +385,7 @@ __global__ void __launch_bounds__(RUN_TPB) ildl_run_kernel(int l0, int l1, const
         const int s = rows ? rows[t] : t;
         const int64_t b = rp[s], e = rp[s + 1];
         A acc = A(0);
-        for (int64_t q = b + lane; q < e; q += 32) acc = fma_(ld_arith(cv + q), y[ci[q]], acc);
+        for (int64_t q = b + lane; q < e; q += 32) acc = fma_(lda<A>(cv + q), y[ci[q]], acc);
         acc = wsum(acc);
         if (lane == 0) y[s] = y[s] - acc;
       }
@@ -398,7 +398,7 @@ __global__ void __launch_bounds__(RUN_TPB) ildl_run_kernel(int l0, int l1, const
       int s = -1;
       if (slot < R) {
         s = rows ? rows[lo + slot] : lo + slot;
-        for (int64_t q = rp[s] + sub * 32 + lane; q < rp[s + 1]; q += 32 * G) acc = fma_(ld_arith(cv + q), y[ci[q]], acc);
+        for (int64_t q = rp[s] + sub * 32 + lane; q < rp[s + 1]; q += 32 * G) acc = fma_(lda<A>(cv + q), y[ci[q]], acc);
       }
       acc = wsum(acc);
       if (lane == 0) part[warp] = acc;
@@ -433,7 +433,7 @@ __global__ void __launch_bounds__(WIDE_TPB) ildl_wide_kernel(int lo, int hi, con
   if (ok) {
     s = rows ? rows[t] : t;
     const int64_t b = rp[s], e = rp[s + 1];
-    for (int64_t q = b + lane; q < e; q += LANES) acc = fma_(ld_arith(cv + q), y[ci[q]], acc);
+    for (int64_t q = b + lane; q < e; q += LANES) acc = fma_(lda<A>(cv + q), y[ci[q]], acc);
   }
   for (int o = LANES / 2; o > 0; o >>= 1) acc = acc + shfl_xor_any(acc, o);
   if (ok && lane == 0) y[s] = y[s] - acc;
@@ -456,8 +456,8 @@ __global__ void __launch_bounds__(WIDE_TPB) tail_ext_kernel(int m, int s_tail, c
   A acc = A(0);
   if (t < m)
     for (int64_t q = rp[t] + lane; q < rp[t + 1]; q += LANES) {
-      if (NC) acc = fma_(ld_arith_nc(cv + q), y[ld_idx_nc(ci + q)], acc);
-      else acc = fma_(ld_arith(cv + q), y[ci[q]], acc);
+      if (NC) acc = fma_(ldan<A>(cv + q), y[ld_idx_nc(ci + q)], acc);
+      else acc = fma_(lda<A>(cv + q), y[ci[q]], acc);
     }
   for (int o = LANES / 2; o > 0; o >>= 1) acc = acc + shfl_xor_any(acc, o);
   if (t < m && lane == 0) out[t] = y[s_tail + t] - acc;
@@ -546,7 +546,7 @@ __global__ void __launch_bounds__(RUN_TPB) tail_run_kernel(int m, int s_tail, in
     assign(0, r, q0, q1, step, G, slot, sub);
     if (q0 < q1) {
       pci = ci[base + q0];
-      pcv = ld_arith(cv + base + q0);
+      pcv = lda<A>(cv + base + q0);
     }
   }
   for (int l = 0; l < nlev; ++l) {
@@ -554,7 +554,7 @@ __global__ void __launch_bounds__(RUN_TPB) tail_run_kernel(int m, int s_tail, in
     A acc = A(0);
     if (q0 < q1) {
       acc = pcv * yt[pci];
-      for (int q = q0 + step; q < q1; q += step) acc = fma_(ld_arith(cv + base + q), yt[ci[base + q]], acc);
+      for (int q = q0 + step; q < q1; q += step) acc = fma_(lda<A>(cv + base + q), yt[ci[base + q]], acc);
     }
     acc = wsum(acc);
     if (R >= RUN_WARPS) {
@@ -562,7 +562,7 @@ __global__ void __launch_bounds__(RUN_TPB) tail_run_kernel(int m, int s_tail, in
       for (int t = lo + warp + RUN_WARPS; t < hi; t += RUN_WARPS) {  // further rows of this warp
         const int rr = rows ? srw[t] : t;
         A a2 = A(0);
-        for (int q = srp[rr] + lane; q < srp[rr + 1]; q += 32) a2 = fma_(ld_arith(cv + base + q), yt[ci[base + q]], a2);
+        for (int q = srp[rr] + lane; q < srp[rr + 1]; q += 32) a2 = fma_(lda<A>(cv + base + q), yt[ci[base + q]], a2);
         a2 = wsum(a2);
         if (lane == 0) yt[rr] = yt[rr] - a2;
       }
@@ -574,7 +574,7 @@ __global__ void __launch_bounds__(RUN_TPB) tail_run_kernel(int m, int s_tail, in
       assign(l + 1, nr, nq0, nq1, nstep, nG, nslot, nsub);
       if (nq0 < nq1) {
         pci = ci[base + nq0];
-        pcv = ld_arith(cv + base + nq0);
+        pcv = lda<A>(cv + base + nq0);
       }
     }
     __syncthreads();
@@ -642,7 +642,7 @@ __global__ void __cluster_dims__(TRI_CL, 1, 1) __launch_bounds__(TRI_TPB)
       const A xv = c < m ? x[c] : A(0);
       const S* e = reinterpret_cast<const S*>(&buf[sl]);
 #pragma unroll
-      for (int v = 0; v < V; ++v) acc[v] = fma_(ld_arith(e + v), xv, acc[v]);
+      for (int v = 0; v < V; ++v) acc[v] = fma_(lda<A>(e + v), xv, acc[v]);
     }
   };
   // One tile per step.  Measured on GB300 (fp32 factor, Anderson model,
@@ -672,6 +672,11 @@ __global__ void __cluster_dims__(TRI_CL, 1, 1) __launch_bounds__(TRI_TPB)
     if (e < m) y[e] = sum;
   }
   cl.sync();  // the other ranks' shared memory stays alive until rank 0 has read it
+}
+
+template <class S, class A>
+static void launch_tri(int items, const int4* it, const S* tiles, const A* x, int m, A* y, cudaStream_t s) {
+  launch_k(tri_cluster_kernel<S, A>, dim3(items), dim3(TRI_TPB), 0, s, it, tiles, x, m, y);
 }
 
 // raise the dynamic shared-memory limit of the tail kernel once per size
@@ -849,8 +854,7 @@ template <class T, class S> void ildl_apply(const DevFactor<S>& F, bool spd, con
       if (B.nt > 0) {
         // right-hand side into xb, then y_B = T xb
         ext(B.m, B.s0, B.ep, B.ei, B.ev, B.nfe, F.xb);
-        launch_k(tri_cluster_kernel<S, A>, dim3(B.nitf), dim3(TRI_TPB), 0, s, (const int4*)B.itf, B.tf,
-                 (const A*)F.xb, B.m, yb);
+        launch_tri<S, A>(B.nitf, (const int4*)B.itf, B.tf, (const A*)F.xb, B.m, yb, s);
       } else if (B.nfe > 0) {
         ext(B.m, B.s0, B.ep, B.ei, B.ev, B.nfe, yb);
       }
@@ -867,8 +871,7 @@ template <class T, class S> void ildl_apply(const DevFactor<S>& F, bool spd, con
       A* yb = F.y + B.s0;
       if (B.nt > 0) {
         ext(B.m, B.s0, B.bp, B.bi, B.bv, B.nbe, F.xb);
-        launch_k(tri_cluster_kernel<S, A>, dim3(B.nitb), dim3(TRI_TPB), 0, s, (const int4*)B.itb, B.tb,
-                 (const A*)F.xb, B.m, yb);
+        launch_tri<S, A>(B.nitb, (const int4*)B.itb, B.tb, (const A*)F.xb, B.m, yb, s);
       } else if (B.nbe > 0) {
         ext(B.m, B.s0, B.bp, B.bi, B.bv, B.nbe, yb);
       }
