@@ -143,15 +143,17 @@ struct Options {
   int fuse_inner = 1;          // inner iterations read their scalars back once (library operators only)
   int revcom_device = 0;       // reverse-communication requests are served on the device copy of X
   int matching = 0;            // first factor level decides with the maximum-product matching scale
-  // factor form (IldlcParams) from coupled_min_n rows on: coupling blocks per
-  // level, the Schur-contribution drop rule, look-ahead pivot deferral and an
-  // exact last level once a level's matrix is a third full
-  int coupling = 1;
+  // factor form (IldlcParams) from coupled_min_n rows on: the Schur-
+  // contribution drop rule, look-ahead pivot deferral and an exact last level
+  // once a level's matrix is a third full; one global L (coupling 0, one
+  // sweep each way) or, with coupling 1, per-level coupling blocks (less
+  // memory, two B-solves per level)
+  int coupling = 0;
   int drop_rule = 1;
   int lookahead = 1;
   double last_droptol = 0.0;
   double last_fill = 1.0 / 3.0;
-  int coupled_min_n = 20000;   // smaller matrices keep one global L (coupling 0, drop rule 0)
+  int coupled_min_n = 20000;   // smaller matrices keep the plain factor (drop rule 0, no look-ahead)
   int factor_verbose = 0;
 };
 static Options g_opt;
@@ -470,7 +472,7 @@ void upload_factor(const IldlcFactor<H>& F, DevFactor<S>& D, cudaStream_t st, Al
   k::ildl_plan(D, lp, up, brs);
   k::ildl_plan_bwd0(D, up, brs);
   CK(cudaStreamSynchronize(st));
-  if (g_opt.verbose) {
+  if (g_opt.verbose || g_opt.factor_verbose) {
     int dense_b = 0;
     for (const auto& B : D.blocks) dense_b += B.nt > 0;
     std::fprintf(stderr,

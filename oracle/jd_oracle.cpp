@@ -36,11 +36,11 @@ static double g_depth_weight = 64.0;
 static double g_drop_schur = -1.0;  // IldlcParams::droptol_schur (negative: its default rule)
 static int g_matching = 0;          // IldlcParams::matching
 // factor form for matrices of at least g_coupled_min_n rows (the library's
-// defaults: coupling blocks, Schur-contribution drop rule, look-ahead pivot
+// defaults: one global L, Schur-contribution drop rule, look-ahead pivot
 // deferral, exact last level once a level's matrix is a third full); smaller
 // ones keep IldlcParams' own
 static int g_drop_rule = 1;         // IldlcParams::drop_rule
-static int g_coupling = 1;          // IldlcParams::coupling
+static int g_coupling = 0;          // IldlcParams::coupling
 static double g_last_droptol = 0;   // IldlcParams::last_droptol
 static double g_last_fill = 1.0 / 3.0;  // IldlcParams::last_fill
 static int g_coupled_min_n = 20000;

@@ -19,8 +19,8 @@ parity tests check every returned eigenvalue against this wider set.
 Matrices: 3-D Anderson model, periodic m^3 lattice, hopping -1, diagonal
 uniform in [-8.25, 8.25] from the seeded splitmix64 stream (seed 0), as the
 benchmark builds them.  Solver settings as the benchmark: ISEARCH = 2,
-sigma = 0, MADSPACE = 25, TOL 1e-10, DROPTOL 1e-3, MEM 15 (the reference's
-Anderson sample), float32 factor.
+sigma = 0, MADSPACE = 25, TOL 1e-10, DROPTOL 1e-3 (the reference's Anderson
+sample), MEM 20, float32 factor.
 
 Run from the repository root (sizes as arguments; 100 takes tens of minutes
 on one core):
@@ -39,7 +39,7 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.dirname(HERE))
 
-KW = dict(isearch=2, sigma=0.0, madspace=25, maxit=100000, tol=1e-10, droptol=1e-3, mem=15.0, icntl=(0, 1, 0, 0, 1))
+KW = dict(isearch=2, sigma=0.0, madspace=25, maxit=100000, tol=1e-10, droptol=1e-3, mem=20.0, icntl=(0, 1, 0, 0, 1))
 LANCZOS_MAX = 40  # largest lattice edge whose sparse LU this script factors
 ORACLE14_MAX = 60  # largest lattice edge with the 14-eigenvalue oracle solve
 

@@ -94,21 +94,24 @@ def test_memory_limit_reports_error(oracle):
 
 
 class _CoupledForm:
-    """The coupling-block form on small matrices (the library uses it from
-    20000 rows on): every level keeps its own L and D, the coupling blocks F
+    """The coupling-block form (option coupling 1, from 20000 rows on) on
+    small matrices: every level keeps its own L and D, the coupling blocks F
     are the level's matrix entries, the last level is exact once a third full."""
 
     def __init__(self, oracle):
         import ctypes as C
         self.lib = oracle.lib()
         self.lib.orc_set_coupled_min_n.argtypes = [C.c_int]
+        self.lib.orc_set_coupling.argtypes = [C.c_int]
 
     def __enter__(self):
         self.lib.orc_set_coupled_min_n(0)
+        self.lib.orc_set_coupling(1)
         return self
 
     def __exit__(self, *exc):
         self.lib.orc_set_coupled_min_n(20000)
+        self.lib.orc_set_coupling(0)
 
 
 @pytest.mark.parametrize("name", ["laplace6", "anderson7", "random_indefinite", "tridiag_zero_diag"])

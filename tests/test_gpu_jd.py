@@ -228,20 +228,85 @@ def test_generalized_harmonic_complex(gpu):
     np.testing.assert_allclose(np.sort(r["eigs"]), ref, rtol=1e-9, atol=1e-12)
 
 
+@pytest.mark.parametrize("coupling", [0, 1])
 @pytest.mark.parametrize("precision", [0, 1])
-def test_anderson_coupled_form(gpu, oracle, precision):
-    """Anderson 28^3 (n = 21952): from 20000 rows the factor keeps each
-    level's L apart and couples the levels through F blocks.  Ten interior
-    eigenvalues against shift-and-invert Lanczos and the oracle (same factor
-    form), residuals at TOL."""
+def test_anderson_large_form(gpu, oracle, coupling, precision):
+    """Anderson 28^3 (n = 21952) with the factor form of 20000 rows and more,
+    one global L (coupling 0) or per-level coupling blocks (coupling 1).  Ten
+    interior eigenvalues against shift-and-invert Lanczos and the oracle (same
+    factor form), residuals at TOL."""
+    import ctypes as C
     from problems import shift_invert_eigs
+    lib = oracle.lib()
+    lib.orc_set_coupling.argtypes = [C.c_int]
     ia, ja, a = M.anderson3d(28, seed=0)
     kw = dict(isearch=2, sigma=0.0, madspace=25, maxit=20000, tol=1e-10, droptol=3e-3, mem=60.0,
               icntl=(0, 1, 0, 0, precision))
-    r = gpu.dpjd((a, ja, ia), 10, **kw)
+    lib.orc_set_coupling(coupling)
+    gpu.set_option("coupling", coupling)
+    try:
+        r = gpu.dpjd((a, ja, ia), 10, **kw)
+        ro = oracle.dpjd(ia, ja, a, 10, **kw)
+    finally:
+        lib.orc_set_coupling(0)
+        gpu.set_option("coupling", 0)
     assert r["info"] == 0 and r["neig"] == 10
     As = M.to_scipy_full(ia, ja, a)
     _close(r["eigs"], shift_invert_eigs(As, 10))
     assert np.all(r["res"] <= 1.1e-10)
-    ro = oracle.dpjd(ia, ja, a, 10, **kw)
     _close(r["eigs"], ro["eigs"])
+
+
+@pytest.mark.parametrize("m", [40, 60])
+def test_anderson_bench_sizes_match_fixtures(gpu, m):
+    """The benchmark's Anderson workload at 40^3 and 60^3 (seed 0, ten
+    eigenpairs closest to 0, TOL 1e-10, float32 factor) against the committed
+    fixtures (tests/golden/make_anderson_fixtures.py): shift-and-invert
+    Lanczos (40^3) and the oracle.  Every returned eigenvalue equals one of
+    the 14 eigenvalues closest to 0 within max(1e-10 |lambda|, 64 eps ||A||),
+    ||A|| <= 6 + 8.25, and at least 9 of the 10 closest are returned: Jacobi-
+    Davidson (the reference's too) can skip one member of a tight cluster and
+    converge to the next eigenvalue instead.  Residuals at TOL."""
+    import json
+    import os
+    with open(os.path.join(os.path.dirname(__file__), "golden", "anderson_eigs.json")) as f:
+        fx = json.load(f)
+    case = fx["cases"][str(m)]
+    ia, ja, a = M.anderson3d(m, disorder=16.5, seed=0)
+    st = fx["settings"]
+    r = gpu.dpjd((a, ja, ia), 10, isearch=st["isearch"], sigma=st["sigma"], madspace=st["madspace"],
+                 maxit=st["maxit"], tol=st["tol"], droptol=st["droptol"], mem=st["mem"], icntl=tuple(st["icntl"]))
+    assert r["info"] == 0 and r["neig"] == 10
+    assert np.all(r["res"] <= 1.1e-10)
+    floor = 64 * np.finfo(float).eps * (6 + 8.25)
+    wide = np.array(case.get("shift_invert14", case.get("oracle14")))
+    closest = wide[np.argsort(np.abs(wide), kind="stable")[:10]]
+    for lam in r["eigs"]:
+        assert np.min(np.abs(wide - lam)) <= max(1e-10 * abs(lam), floor), (lam, wide)
+    found = sum(np.min(np.abs(r["eigs"] - w)) <= max(1e-10 * abs(w), floor) for w in closest)
+    assert found >= 9, (np.sort(r["eigs"]), closest)
+
+
+@pytest.mark.parametrize("m", [32, 64])
+def test_tightbinding_matches_fixtures(gpu, m):
+    """Complex Hermitian tight-binding workload (Peierls phases, phi = 1/17),
+    8 smallest eigenvalues, complex128 outer / complex64 factor, at 32^3 and
+    at the benchmark's 64^3 (n = 262,144), against the committed fixtures
+    (tests/golden/make_tightbinding_fixtures.py): the oracle at both sizes and
+    ARPACK Lanczos at 32^3.  Tolerance max(1e-10 |lambda|, 64 eps ||A||),
+    ||A|| <= 6 + 2; residuals at TOL."""
+    import json
+    import os
+    with open(os.path.join(os.path.dirname(__file__), "golden", "tightbinding_eigs.json")) as f:
+        fx = json.load(f)
+    case = fx["cases"][str(m)]
+    st = fx["settings"]
+    ia, ja, a = M.tight_binding3d(m, phi=1.0 / 17.0, disorder=4.0, seed=1)
+    r = gpu.zpjd((a, ja, ia), 8, isearch=st["isearch"], sigma=st["sigma"], madspace=st["madspace"],
+                 maxit=st["maxit"], tol=st["tol"], droptol=st["droptol"], mem=st["mem"], icntl=tuple(st["icntl"]))
+    assert r["info"] == 0 and r["neig"] == 8
+    floor = 64 * np.finfo(float).eps * 8.0
+    for key in ("lanczos", "oracle"):
+        if key in case:
+            _close(r["eigs"], np.array(case[key]), rel=1e-10, floor=floor)
+    assert np.all(r["res"] <= 1.1e-10)

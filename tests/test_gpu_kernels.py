@@ -93,19 +93,31 @@ def test_ildl_apply_tail_variants_match_oracle(gpu, oracle, variant, precision, 
         assert err <= tol, err
 
 
+@pytest.mark.parametrize("coupling", [0, 1])
 @pytest.mark.parametrize("spd", [False, True])
 @pytest.mark.parametrize("precision,tol", [(0, 1e-11), (1, 2e-5)])
-def test_ildl_apply_coupled_matches_oracle(gpu, oracle, spd, precision, tol):
-    """From 20000 rows on the factor keeps each level's L and D apart with
-    coupling blocks F (the multilevel form of symAMGsol.c:173-330): Anderson
-    28^3 (n = 21952), applied on the GPU as per-level sub-factors, F and F^H,
+def test_ildl_apply_large_form_matches_oracle(gpu, oracle, coupling, spd, precision, tol):
+    """From 20000 rows on the factor defers pivots by look-ahead, drops by
+    Schur contribution and factors its last level exactly; it keeps one global
+    L (coupling 0, default) or each level's L and D apart with coupling blocks
+    F (coupling 1, the multilevel form of symAMGsol.c:173-330, applied on the
+    GPU as per-level sub-factors, F and F^H).  Anderson 28^3 (n = 21952)
     against the oracle's application of the same factor."""
+    import ctypes as C
+    lib = oracle.lib()
+    lib.orc_set_coupling.argtypes = [C.c_int]
     ia, ja, a = M.anderson3d(28, seed=2)
     n = len(ia) - 1
-    F = oracle.Factor(ia, ja, a, shift=0.0, droptol=3e-3, mem=0)
-    assert F.ierr == 0 and F.info()["nlevels"] >= 2
-    B = np.random.default_rng(5).standard_normal((2, n))
-    Xg, info = gpu.ildl_apply((a, ja, ia), B, shift=0.0, droptol=3e-3, spd=spd, precision=precision)
+    lib.orc_set_coupling(coupling)
+    gpu.set_option("coupling", coupling)
+    try:
+        F = oracle.Factor(ia, ja, a, shift=0.0, droptol=3e-3, mem=0)
+        assert F.ierr == 0 and F.info()["nlevels"] >= 2
+        B = np.random.default_rng(5).standard_normal((2, n))
+        Xg, info = gpu.ildl_apply((a, ja, ia), B, shift=0.0, droptol=3e-3, spd=spd, precision=precision)
+    finally:
+        lib.orc_set_coupling(0)
+        gpu.set_option("coupling", 0)
     assert info["nnz_l"] == F.info()["nnz_l"]
     for r in range(2):
         xo = F.apply(B[r], spd=spd)
