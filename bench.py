@@ -534,7 +534,7 @@ def run_gb300(args):
             "clocks": clk,
             "cpu_baseline": cpu,
         }
-        print(json.dumps(_finite(line)))
+        _emit(_finite(line))
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
@@ -633,7 +633,7 @@ def run_reference(args):
             "config": {"workload": w["desc"], "factor_s": factor_s, "matvec_per_solve": int(np.median(iters))},
             "cpu_baseline": {"value": v, "unit": "s", "cores": 1, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    print(json.dumps(line))
+    _emit(line)
 
 
 def _oracle_batch_solve(job):
@@ -699,7 +699,7 @@ def run_reference_batch(args, world):
                        "sampled_problems": len(range(0, args.batch, stride))},
             "cpu_baseline": {"value": v, "unit": "s", "cores": procs, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    print(json.dumps(_finite(line)))
+    _emit(_finite(line))
 
 
 def run_batch(args):
@@ -804,11 +804,28 @@ def run_batch(args):
                        "info_nonzero": int(sum(r["info"] != 0 for r in outs))},
             "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "roofline": roof, "gpu_launches": int(launches), "clocks": clk, "cpu_baseline": cpu}
-    print(json.dumps(_finite(line)))
+    _emit(_finite(line))
+
+
+_RESULT_OUT = None
+
+
+def _emit(line):
+    """Write the one result line to the process's original standard output."""
+    out = _RESULT_OUT or sys.stdout
+    out.write(json.dumps(line) + "\n")
+    out.flush()
 
 
 def main():
+    global _RESULT_OUT
     args = parse()
+    # The solver writes its own messages (factor restarts, IPRINT reports) to
+    # standard output as the reference does; move them to stderr so that
+    # standard output carries the result line alone.
+    sys.stdout.flush()
+    _RESULT_OUT = os.fdopen(os.dup(1), "w")
+    os.dup2(2, 1)
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "batch":

@@ -314,7 +314,7 @@ JDG_API int jdgpu_dpjd_batch(int nprob, const int* n, double* const* a, int* con
  * decisions in the symmetric scale of a maximum-product matching, the role of
  * the reference's MC64 step; 2: also pivots the matching's 2-cycles of that
  * level as 2x2 blocks first; default 0, the level's max-norm equilibration).
- * Factor form for matrices of at least "coupled_min_n" rows (default 20000):
+ * Factor form for matrices of at least "coupled_min_n" rows (default 4096):
  * "coupling" (0, default: one global L, one sweep each way; 1: each level
  * keeps its own L and is coupled to the later levels through the block F of
  * its matrix, applied with two B-solves per level as ILUPACK's multilevel
@@ -326,6 +326,9 @@ JDG_API int jdgpu_dpjd_batch(int nprob, const int* n, double* const* a, int* con
  * dropping; negative: DROPTOL) and "last_fill" (a later level whose matrix is
  * at least this full becomes the last level, default 1/3).  "factor_verbose"
  * (1: one line per factor level and per uploaded sub-factor on stderr).
+ * "plan_launch_us" (default 4) and "plan_tile_gbs" (default 5000): the cost
+ * of one launch and the streaming rate the apply planner weighs when it
+ * chooses which runs of sweep levels become dense tiles.
  * They apply to factors computed, and solves started, after the call. */
 JDG_API void jdgpu_set_option(const char* name, double value);
 

@@ -28,9 +28,9 @@ struct BlockGroup {
 };
 inline std::vector<BlockGroup> plan_dense_blocks(const std::vector<int>& fptr, const std::vector<int64_t>& ent_f,
                                                  const std::vector<int64_t>& ent_b, size_t elem_bytes, int dense_max,
-                                                 double min_saving, double t_bulk = 4e-6) {
+                                                 double min_saving, double t_bulk = 4e-6, double t_launch = 4e-6,
+                                                 double bw = 5.0e12) {
   const int nfl = (int)fptr.size() - 1;
-  const double t_launch = 4e-6, bw = 5.0e12;
   const double eb = (double)elem_bytes + 4;
   auto bytes = [&](int l) { return (double)(ent_f[l] + ent_b[l]) * eb / bw; };
   // level 0 has no entries in the forward sweep: one launch (or step) less

@@ -138,6 +138,8 @@ struct Options {
   int dense_tail = 1;          // solve the deepest levels with their explicit inverse
   int dense_max = 32768;       // at most this many rows in the dense tail
   double dense_min_saving = 100e-6;  // modelled seconds per application the dense blocks must save
+  double plan_launch_us = 4.0;       // the block planner's cost of one launch (microseconds)
+  double plan_tile_gbs = 5000.0;     // and its streaming rate of L entries and tiles (GB/s)
   double drop_schur = -1.0;    // IldlcParams::droptol_schur (negative: its default rule)
   int apply_graph = 0;         // jdgpu_dildl_apply through the captured graph
   int fuse_inner = 1;          // inner iterations read their scalars back once (library operators only)
@@ -153,7 +155,7 @@ struct Options {
   int lookahead = 1;
   double last_droptol = 0.0;
   double last_fill = 1.0 / 3.0;
-  int coupled_min_n = 20000;   // smaller matrices keep the plain factor (drop rule 0, no look-ahead)
+  int coupled_min_n = 4096;    // smaller matrices keep the plain factor (drop rule 0, no look-ahead)
   int factor_verbose = 0;
 };
 static Options g_opt;
@@ -264,7 +266,8 @@ void upload_factor(const IldlcFactor<H>& F, DevFactor<S>& D, cudaStream_t st, Al
         ent_f[l] += lp[s + 1] - lp[s];
         ent_b[l] += up[s + 1] - up[s];
       }
-    groups = plan_dense_blocks(fptr, ent_f, ent_b, sizeof(S), g_opt.dense_max, g_opt.dense_min_saving);
+    groups = plan_dense_blocks(fptr, ent_f, ent_b, sizeof(S), g_opt.dense_max, g_opt.dense_min_saving,
+                               g_opt.plan_launch_us * 1e-6, g_opt.plan_launch_us * 1e-6, g_opt.plan_tile_gbs * 1e9);
     if (!groups.empty()) Lt = groups[0].a;
   } else {
     int acc_rows = 0;
@@ -2089,6 +2092,8 @@ JDG_API void jdgpu_set_option(const char* name, double value) {
   else if (!std::strcmp(name, "dense_tail")) g_opt.dense_tail = (int)value;
   else if (!std::strcmp(name, "dense_max")) g_opt.dense_max = (int)value;
   else if (!std::strcmp(name, "dense_min_saving")) g_opt.dense_min_saving = value;
+  else if (!std::strcmp(name, "plan_launch_us")) g_opt.plan_launch_us = value;
+  else if (!std::strcmp(name, "plan_tile_gbs")) g_opt.plan_tile_gbs = value;
   else if (!std::strcmp(name, "drop_schur")) g_opt.drop_schur = value;
   else if (!std::strcmp(name, "pdl")) k::set_pdl(value != 0);
   else if (!std::strcmp(name, "apply_graph")) g_opt.apply_graph = (int)value;

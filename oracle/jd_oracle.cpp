@@ -43,7 +43,7 @@ static int g_drop_rule = 1;         // IldlcParams::drop_rule
 static int g_coupling = 0;          // IldlcParams::coupling
 static double g_last_droptol = 0;   // IldlcParams::last_droptol
 static double g_last_fill = 1.0 / 3.0;  // IldlcParams::last_fill
-static int g_coupled_min_n = 20000;
+static int g_coupled_min_n = 4096;
 static int g_lookahead = 1;         // IldlcParams::lookahead
 static void factor_form(jdg::IldlcParams& p, int n) {
   if (n < g_coupled_min_n) return;

@@ -94,7 +94,7 @@ def test_memory_limit_reports_error(oracle):
 
 
 class _CoupledForm:
-    """The coupling-block form (option coupling 1, from 20000 rows on) on
+    """The coupling-block form (option coupling 1, from 4096 rows on) on
     small matrices: every level keeps its own L and D, the coupling blocks F
     are the level's matrix entries, the last level is exact once a third full."""
 
@@ -110,7 +110,7 @@ class _CoupledForm:
         return self
 
     def __exit__(self, *exc):
-        self.lib.orc_set_coupled_min_n(20000)
+        self.lib.orc_set_coupled_min_n(4096)
         self.lib.orc_set_coupling(0)
 
 

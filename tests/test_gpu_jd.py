@@ -231,7 +231,7 @@ def test_generalized_harmonic_complex(gpu):
 @pytest.mark.parametrize("coupling", [0, 1])
 @pytest.mark.parametrize("precision", [0, 1])
 def test_anderson_large_form(gpu, oracle, coupling, precision):
-    """Anderson 28^3 (n = 21952) with the factor form of 20000 rows and more,
+    """Anderson 28^3 (n = 21952) with the factor form of 4096 rows and more,
     one global L (coupling 0) or per-level coupling blocks (coupling 1).  Ten
     interior eigenvalues against shift-and-invert Lanczos and the oracle (same
     factor form), residuals at TOL."""
@@ -310,3 +310,28 @@ def test_tightbinding_matches_fixtures(gpu, m):
         if key in case:
             _close(r["eigs"], np.array(case[key]), rel=1e-10, floor=floor)
     assert np.all(r["res"] <= 1.1e-10)
+
+
+def test_anderson_100_cubed_headline(gpu):
+    """The benchmark's headline workload at full size: Anderson 100^3
+    (n = 1e6), ten eigenpairs closest to 0, fp32 factor, DROPTOL 1e-3.  The
+    eigenvalues equal the oracle's complete solve (committed fixture) within
+    max(1e-10 |lambda|, 64 eps ||A||), and every returned pair's residual
+    ||A x - lambda x|| / ||x||, recomputed here in float64 by scipy, is at
+    most 1.2 TOL."""
+    import json
+    import os
+    with open(os.path.join(os.path.dirname(__file__), "golden", "anderson_eigs.json")) as f:
+        fx = json.load(f)
+    st = fx["settings"]
+    ia, ja, a = M.anderson3d(100, disorder=16.5, seed=0)
+    r = gpu.dpjd((a, ja, ia), 10, isearch=st["isearch"], sigma=st["sigma"], madspace=st["madspace"],
+                 maxit=st["maxit"], tol=st["tol"], droptol=st["droptol"], mem=st["mem"], icntl=tuple(st["icntl"]))
+    assert r["info"] == 0 and r["neig"] == 10
+    _close(r["eigs"], np.array(fx["cases"]["100"]["oracle"]), rel=1e-10, floor=64 * np.finfo(float).eps * 14.25)
+    As = M.to_scipy_full(ia, ja, a).tocsr()
+    X = r["x"]
+    for k in range(10):
+        x = X[:, k]
+        res = np.linalg.norm(As @ x - r["eigs"][k] * x) / np.linalg.norm(x)
+        assert res <= 1.2 * st["tol"], (k, res)

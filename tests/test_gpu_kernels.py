@@ -97,7 +97,7 @@ def test_ildl_apply_tail_variants_match_oracle(gpu, oracle, variant, precision, 
 @pytest.mark.parametrize("spd", [False, True])
 @pytest.mark.parametrize("precision,tol", [(0, 1e-11), (1, 2e-5)])
 def test_ildl_apply_large_form_matches_oracle(gpu, oracle, coupling, spd, precision, tol):
-    """From 20000 rows on the factor defers pivots by look-ahead, drops by
+    """From 4096 rows on the factor defers pivots by look-ahead, drops by
     Schur contribution and factors its last level exactly; it keeps one global
     L (coupling 0, default) or each level's L and D apart with coupling blocks
     F (coupling 1, the multilevel form of symAMGsol.c:173-330, applied on the
