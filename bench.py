@@ -326,6 +326,42 @@ def cpu_baseline_sample(J, ia, ja, a, args, gpu_iter, w=None):
                       f"({per_mv * 1e3:.1f} ms/MATVEC) scaled to the GPU solve's {gpu_iter} MATVECs"}
 
 
+def cpu_baseline_own_factor(args, w, gpu_iter):
+    """Oracle iterations for the complex and generalized workloads, whose
+    factors are not exported: the oracle factors the same matrix with its
+    own code on all host threads (untimed, as the reference arm does), then
+    runs the MATVECs that fit --cpu-seconds on one core, scaled to the GPU
+    solve's MATVEC count."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib
+    ia, ja, a = w["A"]
+    extra = {"complex_": True} if w["kind"] == "z" else {"b": w["B"]}
+    O = oracle_lib.lib()
+    O.orc_set_threads.argtypes = [C.c_int]
+    threads = os.cpu_count() or 1
+    O.orc_set_threads(threads)
+    kw = solve_kwargs(args, 1, w)
+    kw["maxit"] = 4
+    t0 = time.perf_counter()
+    oracle_lib.dpjd(ia, ja, a, args.neig, **kw, **extra)
+    factor_s = time.perf_counter() - t0
+    kw = solve_kwargs(args, -1, w)
+    kw["maxit"] = 16
+    t0 = time.perf_counter()
+    r = oracle_lib.dpjd(ia, ja, a, args.neig, **kw, **extra)
+    per_mv = (time.perf_counter() - t0) / max(r["iter"], 1)
+    kw["maxit"] = max(16, int(args.cpu_seconds / per_mv))
+    t0 = time.perf_counter()
+    r = oracle_lib.dpjd(ia, ja, a, args.neig, **kw, **extra)
+    dt = time.perf_counter() - t0
+    it = r["iter"]
+    per_mv = dt / max(it, 1)
+    return {"value": per_mv * gpu_iter, "unit": "s", "cores": 1, "kind": "port",
+            "sample": f"CPU oracle, same matrix, its own factor ({factor_s:.1f} s on {threads} threads, untimed); "
+                      f"{it} MATVECs in {dt:.1f} s on one core ({per_mv * 1e3:.1f} ms/MATVEC) scaled to the GPU "
+                      f"solve's {gpu_iter} MATVECs"}
+
+
 def precision_check(J, w, args, timed, stream, torch):
     """One solve with the factor in float64 (the plain FP64 GPU method) and
     one in bfloat16, reusing the host factor (ICNTL(2) = -1, ICNTL(5) 0 / 2):
@@ -417,7 +453,7 @@ def run_gb300(args):
     t0 = time.perf_counter()
     r = run_solve(J, w, args, 1)
     first_s = time.perf_counter() - t0
-    st = J.stats()
+    st = J.stats(complex_=w["kind"] == "z")
     if r["info"] != 0:
         raise SystemExit(f"first solve failed: INFO={r['info']}")
     for _ in range(max(0, args.warmup - 1)):
@@ -446,15 +482,16 @@ def run_gb300(args):
     # above TOL, as in the reference (JDaux.F:2270-2300); max_res reports it
     ok = all(rr["info"] == 0 and rr["neig"] == args.neig for rr in results)
     eigs = np.sort(results[-1]["eigs"])
-    # roofline of the dominant kernels (preconditioner application) and of SpMV
-    # (real standard problems: the resident matrix and the real factor)
+    # roofline of the dominant kernels (preconditioner application) and of SpMV,
+    # with the last solve's factor and matrix (real or complex state)
     pb = np.full(6, np.nan)
     sb = np.full(4, np.nan)
-    if w["resident"]:
-        L.jdgpu_dprecond_bench.argtypes = [C.c_int, C.c_void_p]
-        L.jdgpu_dprecond_bench(20, pb.ctypes.data_as(C.c_void_p))
-        L.jdgpu_dspmv_bench.argtypes = [C.c_int, C.c_void_p]
-        L.jdgpu_dspmv_bench(50, sb.ctypes.data_as(C.c_void_p))
+    pre = "z" if w["kind"] == "z" else "d"
+    for name, reps, buf in (("jdgpu_%sprecond_bench" % pre, 20, pb), ("jdgpu_%sspmv_bench" % pre, 50, sb)):
+        fn = getattr(L, name)
+        fn.argtypes = [C.c_int, C.c_void_p]
+        if fn(reps, buf.ctypes.data_as(C.c_void_p)) != 0:
+            buf[:] = np.nan
     peak, peak_kind = measured_peaks()
     # achieved bandwidth on the algorithmic bytes of one application (pb[5]:
     # every L entry once per sweep, F and F^H, D, vectors); pb[1] adds what the
@@ -485,9 +522,12 @@ def run_gb300(args):
         torch.cuda.synchronize()
         e2e_s = (time.perf_counter() - t0) / args.steps
     cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu and w["kind"] == "d":
+    if rank == 0 and world == 1 and not args.no_cpu:
         try:
-            cpu = cpu_baseline_sample(J, ia, ja, a, args, int(np.median(iters)), w)
+            if w["kind"] == "d":
+                cpu = cpu_baseline_sample(J, ia, ja, a, args, int(np.median(iters)), w)
+            else:
+                cpu = cpu_baseline_own_factor(args, w, int(np.median(iters)))
         except Exception as ex:  # reported, not fatal
             cpu = {"value": None, "unit": "s", "cores": 1, "kind": "port", "sample": f"failed: {ex}"}
     if rank == 0:

@@ -215,11 +215,16 @@ JDG_API void jdgpu_set_stream(void* stream);
 /* Kernels launched by the library so far (graph replays count their nodes). */
 JDG_API long long jdgpu_launch_count(void);
 
-/* Timing of the last real solve's preconditioner / resident SpMV on the
- * solver stream (no reference counterpart; measurement only).  See
- * driver.cu for the algorithmic byte counts written to out. */
+/* Timing of the last real (d) or complex (z) solve's preconditioner and of
+ * SpMV with its matrix, on the solver stream (no reference counterpart;
+ * measurement only).  precond out: ms per application, bytes streamed,
+ * nnz(L), rows in dense blocks, kernels per application, algorithmic bytes;
+ * spmv out: ms per SpMV, algorithmic bytes, nnz, stored entries.  -1: no
+ * factor (or matrix) on the device. */
 JDG_API int jdgpu_dprecond_bench(int reps, double* out);
 JDG_API int jdgpu_dspmv_bench(int reps, double* out);
+JDG_API int jdgpu_zprecond_bench(int reps, double* out);
+JDG_API int jdgpu_zspmv_bench(int reps, double* out);
 
 /* Copy out the host factor of the last real solve (CPU comparison runs). */
 JDG_API int jdgpu_dfactor_export(int* n_out, long long* nnz_out, double* shift_out, int* perm, long long* lp, int* li,
@@ -314,7 +319,9 @@ JDG_API int jdgpu_dpjd_batch(int nprob, const int* n, double* const* a, int* con
  * decisions in the symmetric scale of a maximum-product matching, the role of
  * the reference's MC64 step; 2: also pivots the matching's 2-cycles of that
  * level as 2x2 blocks first; default 0, the level's max-norm equilibration).
- * Factor form for matrices of at least "coupled_min_n" rows (default 4096):
+ * Factor form for matrices of at least "coupled_min_n" rows (default 4096),
+ * in solves with ISEARCH at least "large_form_isearch" (default 2: interior
+ * eigenvalues; the factor-only and gradient entry points count as 2):
  * "coupling" (0, default: one global L, one sweep each way; 1: each level
  * keeps its own L and is coupled to the later levels through the block F of
  * its matrix, applied with two B-solves per level as ILUPACK's multilevel
@@ -354,7 +361,8 @@ JDG_API int jdgpu_revcom_device_ptr(int complex_, void** xd, void** stream);
  * seconds, upload seconds, preconditioner applications, matvecs, levels,
  * forward depth, backward depth, nnz(L), fill, factorisations, rows of the
  * current device factor solved by dense blocks (or the single-CTA tail), and
- * the number of those blocks. */
+ * the number of those blocks.  jdgpu_reset_stats clears the counters and
+ * times of both. */
 JDG_API void jdgpu_dstats(double* out);
 JDG_API void jdgpu_zstats(double* out);
 JDG_API void jdgpu_reset_stats(void);

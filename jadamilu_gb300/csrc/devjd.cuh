@@ -74,6 +74,7 @@ template <class T> struct Workspace {
     if (need_part > cap_part) {
       if (dpart) CK(cudaFree(dpart));
       CK(cudaMalloc(&dpart, sizeof(T) * need_part));
+      CK(cudaMemset(dpart, 0, sizeof(T) * need_part));  // the reduction's arrival counter starts at zero
       cap_part = need_part;
     }
     N = n;

@@ -156,17 +156,22 @@ struct Options {
   double last_droptol = 0.0;
   double last_fill = 1.0 / 3.0;
   int coupled_min_n = 4096;    // smaller matrices keep the plain factor (drop rule 0, no look-ahead)
+  // a solve takes that form only when its ISEARCH is at least this: 2, the
+  // interior eigenvalues of an indefinite shifted matrix (ISEARCH 0 and 1
+  // factor a matrix shifted below or near the lower end of the spectrum)
+  int large_form_isearch = 2;
   int factor_verbose = 0;
 };
 static Options g_opt;
 
-// the factor options of this library on top of the caller's droptol/condest/mem
-static void factor_options(IldlcParams& p, int n) {
+// the factor options of this library on top of the caller's droptol/condest/mem;
+// isearch: the solve's ISEARCH (2 for the factor-only and gradient entry points)
+static void factor_options(IldlcParams& p, int n, int isearch = 2) {
   p.depth_weight = g_opt.depth_weight;
   p.droptol_schur = g_opt.drop_schur;
   p.matching = g_opt.matching;
   p.verbose = g_opt.factor_verbose;
-  if (n >= g_opt.coupled_min_n) {
+  if (n >= g_opt.coupled_min_n && isearch >= g_opt.large_form_isearch) {
     p.coupling = g_opt.coupling;
     p.drop_rule = g_opt.drop_rule;
     p.last_droptol = g_opt.last_droptol;
@@ -809,7 +814,7 @@ int pjdinit(Global<T>& g, Printer& P, int n, typename HostOf<T>::type* a, int* j
     prm.droptol = DROPTOL;
     prm.condest = condest;
     prm.mem = MEM;
-    factor_options(prm, n);
+    factor_options(prm, n, isearch);
     prm.threads = g.factor_threads;
     double tf0 = wall();
     int ierr = ildlc_factor<H>(n, ia, ja, a, g.shift0, gep ? ib : nullptr, gep ? jb : nullptr, gep ? b : nullptr,
@@ -1899,89 +1904,117 @@ JDG_API void jdgpu_dmatrix_info(long* out) {
 
 JDG_API long long jdgpu_launch_count(void) { return k::launch_count(); }
 
-// Times `reps` applications of the preconditioner built by the last real
-// solve (CUDA events on the solver stream).  out: ms per application,
-// algorithmic bytes per application, nnz(L), tail rows, kernels per application.
+// Times `reps` applications of the last solve's device factor (T: the outer
+// arithmetic, double or complex double) through its captured graph.  out: ms
+// per application, bytes streamed, nnz(L), rows in dense blocks, kernels per
+// application, algorithmic bytes.
+extern "C++" {
+template <class T> static int precond_bench(int reps, double* out) {
+  Global<T>& g = G<T>();
+  if (g.factdgl >= 0) return -1;
+  const long n = g.F.n;
+  cudaStream_t st = g.W.st;
+  T *b, *x;
+  CK(cudaMalloc(&b, sizeof(T) * n));
+  CK(cudaMalloc(&x, sizeof(T) * n));
+  k::fill<T>(n, T(1.0), b, st);
+  auto run = [&]() {
+    if (g.precision == 1) k::ildl_apply_graph<T, typename Global<T>::L>(g.Fs, false, b, x, st);
+    else if (g.precision == 2) k::ildl_apply_graph<T, typename Global<T>::B>(g.Fb, false, b, x, st);
+    else k::ildl_apply_graph<T, T>(g.Fd, false, b, x, st);
+  };
+  for (int r = 0; r < 2; ++r) run();
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  CK(cudaEventRecord(e0, st));
+  for (int r = 0; r < reps; ++r) run();
+  CK(cudaEventRecord(e1, st));
+  CK(cudaEventSynchronize(e1));
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, e0, e1));
+  out[0] = ms / reps;
+  auto fill_out = [&](const auto& D) {
+    out[1] = precond_bytes(D);
+    out[2] = (double)D.nnz_l;
+    out[3] = dense_rows(D);
+    out[4] = (double)D.graph_kernels[0];
+    out[5] = precond_bytes_alg(D);
+  };
+  if (g.precision == 1) fill_out(g.Fs);
+  else if (g.precision == 2) fill_out(g.Fb);
+  else fill_out(g.Fd);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(b);
+  cudaFree(x);
+  return 0;
+}
+}  // extern "C++"
 JDG_API int jdgpu_dprecond_bench(int reps, double* out) {
   try {
-    Global<double>& g = G<double>();
-    if (g.factdgl >= 0) return -1;
-    const long n = g.F.n;
-    cudaStream_t st = g.W.st;
-    double *b, *x;
-    CK(cudaMalloc(&b, sizeof(double) * n));
-    CK(cudaMalloc(&x, sizeof(double) * n));
-    k::fill<double>(n, 1.0, b, st);
-    auto run = [&]() {
-      if (g.precision == 1) k::ildl_apply_graph<double, float>(g.Fs, false, b, x, st);
-      else if (g.precision == 2) k::ildl_apply_graph<double, __nv_bfloat16>(g.Fb, false, b, x, st);
-      else k::ildl_apply_graph<double, double>(g.Fd, false, b, x, st);
-    };
-    for (int r = 0; r < 2; ++r) run();
-    cudaEvent_t e0, e1;
-    CK(cudaEventCreate(&e0));
-    CK(cudaEventCreate(&e1));
-    CK(cudaEventRecord(e0, st));
-    for (int r = 0; r < reps; ++r) run();
-    CK(cudaEventRecord(e1, st));
-    CK(cudaEventSynchronize(e1));
-    float ms = 0;
-    CK(cudaEventElapsedTime(&ms, e0, e1));
-    out[0] = ms / reps;
-    auto fill_out = [&](const auto& D) {
-      out[1] = precond_bytes(D);
-      out[2] = (double)D.nnz_l;
-      out[3] = dense_rows(D);
-      out[4] = (double)D.graph_kernels[0];
-      out[5] = precond_bytes_alg(D);
-    };
-    if (g.precision == 1) fill_out(g.Fs);
-    else if (g.precision == 2) fill_out(g.Fb);
-    else fill_out(g.Fd);
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    cudaFree(b);
-    cudaFree(x);
-    return 0;
+    return precond_bench<double>(reps, out);
   } catch (std::exception& e) {
     std::fprintf(stderr, "jdgpu_dprecond_bench: %s\n", e.what());
     return -99;
   }
 }
+JDG_API int jdgpu_zprecond_bench(int reps, double* out) {
+  try {
+    return precond_bench<zc>(reps, out);
+  } catch (std::exception& e) {
+    std::fprintf(stderr, "jdgpu_zprecond_bench: %s\n", e.what());
+    return -99;
+  }
+}
 
-// Times `reps` SpMVs with the resident matrix.  out: ms per SpMV, algorithmic
-// bytes (full-matrix values and column indices, slice pointers, x and y).
+// Times `reps` SpMVs with the last solve's (or the resident) matrix.  out: ms
+// per SpMV, algorithmic bytes (full-matrix values and column indices, slice
+// pointers, x and y), nnz, stored entries.
+extern "C++" {
+template <class T> static int spmv_bench(int reps, double* out) {
+  Global<T>& g = G<T>();
+  const long n = g.A.n;
+  if (n <= 0) return -1;
+  cudaStream_t st = g.W.st;
+  T *x, *y;
+  CK(cudaMalloc(&x, sizeof(T) * n));
+  CK(cudaMalloc(&y, sizeof(T) * n));
+  k::fill<T>(n, T(1.0), x, st);
+  for (int r = 0; r < 2; ++r) k::spmv<T>(g.A, x, y, st);
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  CK(cudaEventRecord(e0, st));
+  for (int r = 0; r < reps; ++r) k::spmv<T>(g.A, x, y, st);
+  CK(cudaEventRecord(e1, st));
+  CK(cudaEventSynchronize(e1));
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, e0, e1));
+  out[0] = ms / reps;
+  out[1] = (double)g.A.nnz * (4.0 + sizeof(T)) + 8.0 * (g.A.nslices + 1) + 2.0 * sizeof(T) * n;
+  out[2] = (double)g.A.nnz;
+  out[3] = (double)g.A.stored;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(x);
+  cudaFree(y);
+  return 0;
+}
+}  // extern "C++"
 JDG_API int jdgpu_dspmv_bench(int reps, double* out) {
   try {
-    Global<double>& g = G<double>();
-    const long n = g.A.n;
-    if (n <= 0) return -1;
-    cudaStream_t st = g.W.st;
-    double *x, *y;
-    CK(cudaMalloc(&x, sizeof(double) * n));
-    CK(cudaMalloc(&y, sizeof(double) * n));
-    k::fill<double>(n, 1.0, x, st);
-    for (int r = 0; r < 2; ++r) k::spmv<double>(g.A, x, y, st);
-    cudaEvent_t e0, e1;
-    CK(cudaEventCreate(&e0));
-    CK(cudaEventCreate(&e1));
-    CK(cudaEventRecord(e0, st));
-    for (int r = 0; r < reps; ++r) k::spmv<double>(g.A, x, y, st);
-    CK(cudaEventRecord(e1, st));
-    CK(cudaEventSynchronize(e1));
-    float ms = 0;
-    CK(cudaEventElapsedTime(&ms, e0, e1));
-    out[0] = ms / reps;
-    out[1] = (double)g.A.nnz * 12.0 + 8.0 * (g.A.nslices + 1) + 16.0 * n;
-    out[2] = (double)g.A.nnz;
-    out[3] = (double)g.A.stored;
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    cudaFree(x);
-    cudaFree(y);
-    return 0;
+    return spmv_bench<double>(reps, out);
   } catch (std::exception& e) {
     std::fprintf(stderr, "jdgpu_dspmv_bench: %s\n", e.what());
+    return -99;
+  }
+}
+JDG_API int jdgpu_zspmv_bench(int reps, double* out) {
+  try {
+    return spmv_bench<zc>(reps, out);
+  } catch (std::exception& e) {
+    std::fprintf(stderr, "jdgpu_zspmv_bench: %s\n", e.what());
     return -99;
   }
 }
@@ -2106,6 +2139,7 @@ JDG_API void jdgpu_set_option(const char* name, double value) {
   else if (!std::strcmp(name, "last_droptol")) g_opt.last_droptol = value;
   else if (!std::strcmp(name, "last_fill")) g_opt.last_fill = value;
   else if (!std::strcmp(name, "coupled_min_n")) g_opt.coupled_min_n = (int)value;
+  else if (!std::strcmp(name, "large_form_isearch")) g_opt.large_form_isearch = (int)value;
   else if (!std::strcmp(name, "lookahead")) g_opt.lookahead = (int)value;
   else if (!std::strcmp(name, "factor_verbose")) g_opt.factor_verbose = (int)value;
 }
@@ -2148,6 +2182,10 @@ JDG_API void jdgpu_reset_stats(void) {
   g.t_factor = g.t_upload = 0;
   g.n_precond = g.n_matvec = 0;
   g.nfactor = 0;
+  Global<zc>& z = G<zc>();
+  z.t_factor = z.t_upload = 0;
+  z.n_precond = z.n_matvec = 0;
+  z.nfactor = 0;
 }
 
 
@@ -2196,6 +2234,7 @@ JDG_API int jdgpu_deigvec_grad(int n, const int* ia, const int* ja, const double
     double *dsm, *dpart;
     CK(cudaMalloc(&dsm, sizeof(double) * 4));
     CK(cudaMalloc(&dpart, sizeof(double) * k::mdot_partial_size(n, 1)));
+    CK(cudaMemset(dpart, 0, sizeof(double) * k::mdot_partial_size(n, 1)));
     CK(cudaMemcpyAsync(vec[X], xin, vb, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(vec[G], g, vb, cudaMemcpyHostToDevice, st));
     if (bdiag) CK(cudaMemcpyAsync(vec[BD], bdiag, vb, cudaMemcpyHostToDevice, st));

@@ -33,6 +33,26 @@ __device__ __forceinline__ void pdl_begin() {
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
   asm volatile("griddepcontrol.wait;" ::: "memory");
 }
+// The two halves of pdl_begin, for kernels that load their factor data
+// (never written while the preconditioner runs) before waiting for the
+// predecessor's results: those loads overlap the predecessor's tail.
+__device__ __forceinline__ void pdl_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+// Asks the TMA unit to bring [p, p + bytes) into L2 and returns at once (a
+// hint: nothing waits for it or reads it back).  Only the 16-byte aligned
+// interior of the range is requested, in pieces of at most 64 KB, so no byte
+// outside [p, p + bytes) is touched.
+__device__ __forceinline__ void l2_prefetch(const void* p, size_t bytes) {
+  size_t a = __cvta_generic_to_global(p);
+  size_t e = a + bytes;
+  a = (a + 15) & ~(size_t)15;
+  e &= ~(size_t)15;
+  while (a < e) {
+    const unsigned sz = (unsigned)(e - a < 65536 ? e - a : 65536);
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a), "r"(sz) : "memory");
+    a += sz;
+  }
+}
 static bool g_pdl = true;
 void set_pdl(bool on) { g_pdl = on; }
 template <class... Params, class... Args>
@@ -52,17 +72,52 @@ static void launch_k(void (*kern)(Params...), dim3 grid, dim3 block, size_t smem
 static inline int nblk(long n, int tpb = TPB) { return (int)std::max<long>(1, (n + tpb - 1) / tpb); }
 
 // ---------------------------------------------------------------- SpMV ----
+// The first kSellPre entries of a row (SELL-32: entry j of a slice's row at
+// 32 j + lane) are loaded before waiting for the predecessor that writes x,
+// then gathered together and added in entry order, as one at a time.
+constexpr int kSellPre = 8;
+template <class T> struct SellBatch {
+  int c[kSellPre];
+  T v[kSellPre];
+};
+template <class T>
+__device__ __forceinline__ void sell_load(SellBatch<T>& b, int64_t q, int64_t e, const int* __restrict__ col,
+                                          const T* __restrict__ val) {
+#pragma unroll
+  for (int u = 0; u < kSellPre; ++u) {
+    const int64_t qq = q + 32 * u;
+    if (qq < e) {
+      b.c[u] = __ldg(col + qq);
+      b.v[u] = val[qq];
+    } else {
+      b.c[u] = -1;
+      b.v[u] = T(0);
+    }
+  }
+}
+template <class T> __device__ __forceinline__ T sell_use(const SellBatch<T>& b, const T* __restrict__ x, T acc) {
+  T w[kSellPre];
+#pragma unroll
+  for (int u = 0; u < kSellPre; ++u) w[u] = b.c[u] >= 0 ? x[b.c[u]] : T(0);
+#pragma unroll
+  for (int u = 0; u < kSellPre; ++u)
+    if (b.c[u] >= 0) acc = fma_(b.v[u], w[u], acc);
+  return acc;
+}
 template <class T>
 __global__ void __launch_bounds__(TPB) spmv_sell_kernel(int n, const int64_t* __restrict__ sptr,
                                                         const int* __restrict__ col, const T* __restrict__ val,
                                                         const T* __restrict__ x, T* __restrict__ y) {
-  pdl_begin();
+  pdl_launch();
   int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= n) return;
   int sl = r >> 5, lane = r & 31;
   int64_t b = sptr[sl], e = sptr[sl + 1];
-  T acc = T(0);
-  for (int64_t q = b + lane; q < e; q += 32) acc = fma_(val[q], x[__ldg(col + q)], acc);
+  SellBatch<T> first;
+  sell_load(first, b + lane, e, col, val);
+  pdl_wait();
+  T acc = sell_use(first, x, T(0));
+  for (int64_t q = b + lane + kSellPre * 32; q < e; q += 32) acc = fma_(val[q], x[__ldg(col + q)], acc);
   y[r] = acc;
 }
 template <class T> void spmv(const SellMatrix<T>& A, const T* x, T* y, cudaStream_t s) {
@@ -74,13 +129,16 @@ template <class T>
 __global__ void __launch_bounds__(TPB) spmv_shift_kernel(int n, const int64_t* __restrict__ sptr,
                                                          const int* __restrict__ col, const T* __restrict__ val,
                                                          T a, const T* __restrict__ x, T* __restrict__ y) {
-  pdl_begin();
+  pdl_launch();
   int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= n) return;
   int sl = r >> 5, lane = r & 31;
   int64_t b = sptr[sl], e = sptr[sl + 1];
-  T acc = T(0);
-  for (int64_t q = b + lane; q < e; q += 32) acc = fma_(val[q], x[__ldg(col + q)], acc);
+  SellBatch<T> first;
+  sell_load(first, b + lane, e, col, val);
+  pdl_wait();
+  T acc = sell_use(first, x, T(0));
+  for (int64_t q = b + lane + kSellPre * 32; q < e; q += 32) acc = fma_(val[q], x[__ldg(col + q)], acc);
   y[r] = fma_(a, x[r], acc);
 }
 template <class T> void spmv_shift(const SellMatrix<T>& A, T a, const T* x, T* y, cudaStream_t s) {
@@ -162,6 +220,13 @@ __device__ __forceinline__ double shfl_xor_any(double v, int o) { return __shfl_
 __device__ __forceinline__ cc shfl_xor_any(cc v, int o) { return cc(shfl_xor_any(v.x, o), shfl_xor_any(v.y, o)); }
 __device__ __forceinline__ zc shfl_xor_any(zc v, int o) { return zc(shfl_xor_any(v.x, o), shfl_xor_any(v.y, o)); }
 
+// loads that bypass L1 (data another CTA of the same launch wrote)
+__device__ __forceinline__ double ldcg_(const double* p) { return __ldcg(p); }
+__device__ __forceinline__ zc ldcg_(const zc* p) {
+  const double2 v = __ldcg(reinterpret_cast<const double2*>(p));
+  return zc(v.x, v.y);
+}
+
 constexpr int MD_CH = 8;  // columns per pass
 // Long vectors: up to two rows per thread, enough CTAs in flight to stream V
 // at full bandwidth.  Vectors under 4096 rows keep one CTA per 2048 rows, the
@@ -172,12 +237,25 @@ static inline int md_grid(long n) {
   return (int)std::min<long>((n + 511) / 512, 152L * 8);
 }
 
-long mdot_partial_size(long n, int k) { return (long)md_grid(n) * ((k + MD_CH - 1) / MD_CH) * MD_CH; }
+// The partials follow a 16-byte arrival counter at the start of the buffer
+// (zero when the buffer is allocated; the last CTA of each call resets it).
+constexpr int MD_HEAD = 16;
+long mdot_partial_size(long n, int k) {
+  return (long)md_grid(n) * ((k + MD_CH - 1) / MD_CH) * MD_CH + 2;  // + the counter (2 doubles or 1 complex)
+}
 
+// V^H w in one launch: every CTA writes its per-column partial sums, and the
+// CTA that arrives last (a counter, no waiting) adds them per column in the
+// fixed order of a second pass (strided over TPB threads, then the warp tree),
+// so the result does not depend on which CTA is last.
 template <class T>
-__global__ void __launch_bounds__(TPB) mdot_partial_kernel(long n, int k, const T* __restrict__ V, long ldv,
-                                                           const T* __restrict__ w, T* __restrict__ partial) {
+__global__ void __launch_bounds__(TPB) mdot_kernel(long n, int k, const T* __restrict__ V, long ldv,
+                                                   const T* __restrict__ w, unsigned char* __restrict__ buf,
+                                                   T* __restrict__ out) {
   pdl_begin();
+  unsigned* count = reinterpret_cast<unsigned*>(buf);
+  T* partial = reinterpret_cast<T*>(buf + MD_HEAD);
+  const int g = gridDim.x;
   const int c0 = blockIdx.y * MD_CH;
   const int nc = min(MD_CH, k - c0);
   T acc[MD_CH];
@@ -190,6 +268,7 @@ __global__ void __launch_bounds__(TPB) mdot_partial_kernel(long n, int k, const 
       if (j < nc) acc[j] = fma_(cj(V[i + (long)(c0 + j) * ldv]), wi, acc[j]);
   }
   __shared__ T red[TPB / 32][MD_CH];
+  __shared__ bool last;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
   for (int j = 0; j < MD_CH; ++j) {
@@ -201,32 +280,37 @@ __global__ void __launch_bounds__(TPB) mdot_partial_kernel(long n, int k, const 
   if (threadIdx.x < MD_CH) {
     T v = T(0);
     for (int q = 0; q < TPB / 32; ++q) v += red[q][threadIdx.x];
-    partial[(long)(c0 + threadIdx.x) * gridDim.x + blockIdx.x] = v;
+    partial[(long)(c0 + threadIdx.x) * g + blockIdx.x] = v;
+    __threadfence();
   }
-}
-template <class T>
-__global__ void __launch_bounds__(TPB) mdot_final_kernel(int g, const T* __restrict__ partial, T* __restrict__ out) {
-  pdl_begin();
-  const int c = blockIdx.x;
-  T v = T(0);
-  for (int q = threadIdx.x; q < g; q += TPB) v += partial[(long)c * g + q];
-  __shared__ T red[TPB / 32];
-  for (int o = 16; o > 0; o >>= 1) v += shfl_down(v, o);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
   __syncthreads();
-  if (threadIdx.x == 0) {
-    T t = T(0);
-    for (int q = 0; q < TPB / 32; ++q) t += red[q];
-    out[c] = t;
+  if (threadIdx.x == 0) last = atomicAdd(count, 1u) == (unsigned)(g * gridDim.y) - 1;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  __shared__ T fin[TPB / 32];
+  for (int c = 0; c < k; ++c) {
+    T v = T(0);
+    for (int q = threadIdx.x; q < g; q += TPB) v += ldcg_(partial + (long)c * g + q);
+    for (int o = 16; o > 0; o >>= 1) v += shfl_down(v, o);
+    if (lane == 0) fin[wid] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      T t = T(0);
+      for (int q = 0; q < TPB / 32; ++q) t += fin[q];
+      out[c] = t;
+    }
+    __syncthreads();
   }
+  if (threadIdx.x == 0) *count = 0u;
 }
 template <class T> void mdot(long n, int k, const T* V, long ldv, const T* w, T* out, T* partial, cudaStream_t s) {
   if (k <= 0) return;
   int g = md_grid(n);
   dim3 grid(g, (k + MD_CH - 1) / MD_CH);
-  launch_k(mdot_partial_kernel<T>, dim3(grid), dim3(TPB), 0, s, n, k, V, ldv, w, partial);
-  launch_k(mdot_final_kernel<T>, dim3(k), dim3(TPB), 0, s, g, partial, out);
-  g_launches += 2;
+  launch_k(mdot_kernel<T>, dim3(grid), dim3(TPB), 0, s, n, k, V, ldv, w, reinterpret_cast<unsigned char*>(partial),
+           out);
+  g_launches += 1;
 }
 
 // ------------------------------------------------------ V y (tall-skinny) ----
@@ -325,32 +409,95 @@ template <class T> void diagsolve(long n, const double* d, const T* rhs, T* sol,
 }
 
 // ------------------------------------------------ multilevel LDL^H apply ----
+// Entries q, q + step, ... (below e) of a row, kUnr at a time: a batch's
+// column indices and values are loaded together, then its gathers of y, and
+// the products are added in entry order, so the roundings are those of one
+// entry at a time while kUnr dependent load chains are in flight.
+constexpr int kUnr = 4;
+template <class A> struct EntBatch {
+  int c[kUnr];
+  A v[kUnr];
+};
+template <bool NC, class A, class S>
+__device__ __forceinline__ void ent_load(EntBatch<A>& b, int64_t q, int64_t e, int step, const int* __restrict__ ci,
+                                         const S* __restrict__ cv) {
+#pragma unroll
+  for (int u = 0; u < kUnr; ++u) {
+    const int64_t qq = q + (int64_t)u * step;
+    if (qq < e) {
+      b.c[u] = NC ? ld_idx_nc(ci + qq) : ci[qq];
+      b.v[u] = NC ? ldan<A>(cv + qq) : lda<A>(cv + qq);
+    } else {
+      b.c[u] = -1;
+      b.v[u] = A(0);
+    }
+  }
+}
+template <class A> __device__ __forceinline__ A ent_use(const EntBatch<A>& b, const A* y, A acc) {
+  A w[kUnr];
+#pragma unroll
+  for (int u = 0; u < kUnr; ++u) w[u] = b.c[u] >= 0 ? y[b.c[u]] : A(0);
+#pragma unroll
+  for (int u = 0; u < kUnr; ++u)
+    if (b.c[u] >= 0) acc = fma_(b.v[u], w[u], acc);
+  return acc;
+}
+// entries [q, e) of a row beyond its first batch, into L2 ahead of use
+template <class S>
+__device__ __forceinline__ void prefetch_rest(int64_t q, int64_t e, const int* __restrict__ ci,
+                                              const S* __restrict__ cv) {
+  if (q < e) {
+    l2_prefetch(ci + q, sizeof(int) * (size_t)(e - q));
+    l2_prefetch(cv + q, sizeof(S) * (size_t)(e - q));
+  }
+}
+template <bool NC, class A, class S>
+__device__ __forceinline__ A ent_dot(int64_t q, int64_t e, int step, const int* __restrict__ ci,
+                                     const S* __restrict__ cv, const A* y, A acc) {
+  for (; q < e; q += (int64_t)kUnr * step) {
+    EntBatch<A> b;
+    ent_load<NC>(b, q, e, step, ci, cv);
+    acc = ent_use(b, y, acc);
+  }
+  return acc;
+}
+
 template <class T, class A>
 __global__ void ildl_gather_kernel(int n, const int* __restrict__ orig, const T* __restrict__ b, A* __restrict__ y) {
-  pdl_begin();
+  pdl_launch();
   int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s < n) y[s] = cvt<A>(b[orig[s]]);
+  if (s >= n) return;
+  const int o = orig[s];
+  pdl_wait();
+  y[s] = cvt<A>(b[o]);
 }
 template <class T, class A>
 __global__ void ildl_scatter_kernel(int n, const int* __restrict__ orig, const A* __restrict__ y, T* __restrict__ x) {
-  pdl_begin();
+  pdl_launch();
   int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s < n) x[orig[s]] = cvt<T>(y[s]);
+  if (s >= n) return;
+  const int o = orig[s];
+  pdl_wait();
+  x[o] = cvt<T>(y[s]);
 }
 template <class S, class A>
 __global__ void ildl_dsolve_kernel(int n, const signed char* __restrict__ blk, const int* __restrict__ partner,
                                    const S* __restrict__ dv, const S* __restrict__ dof, A* __restrict__ y) {
-  pdl_begin();
+  pdl_launch();
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
   signed char b = blk[s];
   if (b == 1) {
-    y[s] = lda<A>(dv + s) * y[s];
+    const A d = lda<A>(dv + s);
+    pdl_wait();
+    y[s] = d * y[s];
   } else if (b == 2) {
-    int t = partner[s];
-    A a0 = y[s], a1 = y[t], o = lda<A>(dof + s);
-    y[s] = fma_(lda<A>(dv + s), a0, o * a1);
-    y[t] = fma_(cj(o), a0, lda<A>(dv + t) * a1);
+    const int t = partner[s];
+    const A o = lda<A>(dof + s), d0 = lda<A>(dv + s), d1 = lda<A>(dv + t);
+    pdl_wait();
+    A a0 = y[s], a1 = y[t];
+    y[s] = fma_(d0, a0, o * a1);
+    y[t] = fma_(cj(o), a0, d1 * a1);
   }
 }
 // A run of narrow levels [l0, l1) in one CTA: a warp per row, levels
@@ -384,8 +531,7 @@ __global__ void __launch_bounds__(RUN_TPB) ildl_run_kernel(int l0, int l1, const
       for (int t = lo + warp; t < hi; t += RUN_WARPS) {
         const int s = rows ? rows[t] : t;
         const int64_t b = rp[s], e = rp[s + 1];
-        A acc = A(0);
-        for (int64_t q = b + lane; q < e; q += 32) acc = fma_(lda<A>(cv + q), y[ci[q]], acc);
+        A acc = ent_dot<false>(b + lane, e, 32, ci, cv, (const A*)y, A(0));
         acc = wsum(acc);
         if (lane == 0) y[s] = y[s] - acc;
       }
@@ -398,7 +544,7 @@ __global__ void __launch_bounds__(RUN_TPB) ildl_run_kernel(int l0, int l1, const
       int s = -1;
       if (slot < R) {
         s = rows ? rows[lo + slot] : lo + slot;
-        for (int64_t q = rp[s] + sub * 32 + lane; q < rp[s + 1]; q += 32 * G) acc = fma_(lda<A>(cv + q), y[ci[q]], acc);
+        acc = ent_dot<false>(rp[s] + sub * 32 + lane, rp[s + 1], 32 * G, ci, cv, (const A*)y, acc);
       }
       acc = wsum(acc);
       if (lane == 0) part[warp] = acc;
@@ -423,18 +569,24 @@ template <class S, class A, int LANES>
 __global__ void __launch_bounds__(WIDE_TPB) ildl_wide_kernel(int lo, int hi, const int* __restrict__ rows,
                                                             const int64_t* __restrict__ rp, const int* __restrict__ ci,
                                                             const S* __restrict__ cv, A* __restrict__ y) {
-  pdl_begin();
+  pdl_launch();
   const int g = blockIdx.x * (WIDE_TPB / LANES) + (threadIdx.x / LANES);
   const int lane = threadIdx.x % LANES;
   const int t = lo + g;
   const bool ok = t < hi;
   int s = 0;
-  A acc = A(0);
+  int64_t b = 0, e = 0;
   if (ok) {
     s = rows ? rows[t] : t;
-    const int64_t b = rp[s], e = rp[s + 1];
-    for (int64_t q = b + lane; q < e; q += LANES) acc = fma_(lda<A>(cv + q), y[ci[q]], acc);
+    b = rp[s] + lane;
+    e = rp[s + 1];
+    if (lane == 0) prefetch_rest(b + kUnr * LANES, e, ci, cv);
   }
+  EntBatch<A> first;
+  ent_load<false>(first, b, e, LANES, ci, cv);
+  pdl_wait();
+  A acc = ent_use(first, (const A*)y, A(0));
+  acc = ent_dot<false>(b + kUnr * LANES, e, LANES, ci, cv, (const A*)y, acc);
   for (int o = LANES / 2; o > 0; o >>= 1) acc = acc + shfl_xor_any(acc, o);
   if (ok && lane == 0) y[s] = y[s] - acc;
 }
@@ -450,15 +602,20 @@ template <class S, class A, int LANES, bool NC>
 __global__ void __launch_bounds__(WIDE_TPB) tail_ext_kernel(int m, int s_tail, const int64_t* __restrict__ rp,
                                                            const int* __restrict__ ci, const S* __restrict__ cv,
                                                            const A* y, A* out) {
-  pdl_begin();
+  pdl_launch();
   const int t = blockIdx.x * (WIDE_TPB / LANES) + (threadIdx.x / LANES);
   const int lane = threadIdx.x % LANES;
-  A acc = A(0);
-  if (t < m)
-    for (int64_t q = rp[t] + lane; q < rp[t + 1]; q += LANES) {
-      if (NC) acc = fma_(ldan<A>(cv + q), y[ld_idx_nc(ci + q)], acc);
-      else acc = fma_(lda<A>(cv + q), y[ci[q]], acc);
-    }
+  int64_t b = 0, e = 0;
+  if (t < m) {
+    b = rp[t] + lane;
+    e = rp[t + 1];
+    if (lane == 0) prefetch_rest(b + kUnr * LANES, e, ci, cv);
+  }
+  EntBatch<A> first;
+  ent_load<NC>(first, b, e, LANES, ci, cv);
+  pdl_wait();
+  A acc = ent_use(first, y, A(0));
+  acc = ent_dot<NC>(b + kUnr * LANES, e, LANES, ci, cv, y, acc);
   for (int o = LANES / 2; o > 0; o >>= 1) acc = acc + shfl_xor_any(acc, o);
   if (t < m && lane == 0) out[t] = y[s_tail + t] - acc;
 }
@@ -615,7 +772,7 @@ template <class S, class A>
 __global__ void __cluster_dims__(TRI_CL, 1, 1) __launch_bounds__(TRI_TPB)
     tri_cluster_kernel(const int4* __restrict__ items, const S* __restrict__ tiles, const A* __restrict__ x, int m,
                        A* __restrict__ y) {
-  pdl_begin();
+  pdl_launch();
   namespace cg = cooperative_groups;
   cg::cluster_group cl = cg::this_cluster();
   constexpr int V = 16 / sizeof(S);
@@ -649,9 +806,14 @@ __global__ void __cluster_dims__(TRI_CL, 1, 1) __launch_bounds__(TRI_TPB)
   // ms per application): 40^3 0.220 -> 0.198 with these loads instead of
   // __ldg, 50^3 unchanged; issuing the next tile's loads before the current
   // tile's products made 50^3 slower (0.387 -> 0.410).
+  // the first tile is read, and the others requested into L2, while the
+  // predecessor (which writes x) finishes
+  uint4 b0[NS];
+  if (cnt > 1 && threadIdx.x == 0) l2_prefetch(tp + 64 * 64 / V, sizeof(S) * 64 * 64 * (size_t)(cnt - 1));
+  if (cnt > 0) load(0, b0);
+  pdl_wait();
   for (int k = 0; k < cnt; ++k) {
-    uint4 b0[NS];
-    load(k, b0);
+    if (k > 0) load(k, b0);
     use(k, b0);
   }
 #pragma unroll

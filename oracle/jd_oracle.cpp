@@ -44,9 +44,10 @@ static int g_coupling = 0;          // IldlcParams::coupling
 static double g_last_droptol = 0;   // IldlcParams::last_droptol
 static double g_last_fill = 1.0 / 3.0;  // IldlcParams::last_fill
 static int g_coupled_min_n = 4096;
+static int g_large_form_isearch = 2;  // solves take that form with ISEARCH at least this
 static int g_lookahead = 1;         // IldlcParams::lookahead
-static void factor_form(jdg::IldlcParams& p, int n) {
-  if (n < g_coupled_min_n) return;
+static void factor_form(jdg::IldlcParams& p, int n, int isearch = 2) {
+  if (n < g_coupled_min_n || isearch < g_large_form_isearch) return;
   p.lookahead = g_lookahead;
   p.coupling = g_coupling;
   p.drop_rule = g_drop_rule;
@@ -356,7 +357,7 @@ int pjdinit(Global<T>& g, int n, T* a, int* ja, int* ia, const T* b, const int* 
     prm.depth_weight = g_depth_weight;
     prm.droptol_schur = g_drop_schur;
     prm.matching = g_matching;
-    factor_form(prm, n);
+    factor_form(prm, n, isearch);
     prm.verbose = std::getenv("JDG_FACTOR_VERBOSE") ? 1 : 0;
     if (g_dense_min_rows >= 0) prm.dense_min_rows = g_dense_min_rows;
     prm.droptol = DROPTOL;
@@ -757,6 +758,7 @@ void orc_set_last_level(double droptol, double fill) {
   orc::g_last_fill = fill;
 }
 void orc_set_coupled_min_n(int v) { orc::g_coupled_min_n = v; }
+void orc_set_large_form_isearch(int v) { orc::g_large_form_isearch = v; }
 void orc_set_lookahead(int v) { orc::g_lookahead = v; }
 // The dense-block inverse tiles (project code under test): L is unit lower
 // triangular of order m given by rows rp/ci/cv (strictly lower, local

@@ -312,6 +312,30 @@ def test_tightbinding_matches_fixtures(gpu, m):
     assert np.all(r["res"] <= 1.1e-10)
 
 
+@pytest.mark.parametrize("m", [128, 512])
+def test_fem_matches_fixtures(gpu, m):
+    """Generalized FEM workload K x = lambda M x (P1, lognormal conductivity,
+    lumped mass), 6 smallest eigenvalues, float64, at 128^2 nodes and at the
+    benchmark's 512^2 (n = 260,100), against the committed fixtures
+    (tests/golden/make_fem_fixtures.py): the oracle and ARPACK
+    shift-and-invert at both sizes.  Tolerance max(1e-10 |lambda|, 64 eps
+    lambda_max) with lambda_max the sixth eigenvalue."""
+    import json
+    import os
+    with open(os.path.join(os.path.dirname(__file__), "golden", "fem_eigs.json")) as f:
+        fx = json.load(f)
+    case = fx["cases"][str(m)]
+    st = fx["settings"]
+    K, Mm = M.fem_p1(m, sigma=0.5, seed=3)
+    r = gpu.dpjd_gep((K[2], K[1], K[0]), (Mm[2], Mm[1], Mm[0]), 6, isearch=st["isearch"], sigma=st["sigma"],
+                     madspace=st["madspace"], maxit=st["maxit"], tol=st["tol"], droptol=st["droptol"], mem=st["mem"],
+                     icntl=tuple(st["icntl"]))
+    assert r["info"] == 0 and r["neig"] == 6
+    floor = 64 * np.finfo(float).eps * max(case["oracle"])
+    for key in ("shift_invert", "oracle"):
+        _close(r["eigs"], np.array(case[key]), rel=1e-10, floor=floor)
+
+
 def test_anderson_100_cubed_headline(gpu):
     """The benchmark's headline workload at full size: Anderson 100^3
     (n = 1e6), ten eigenpairs closest to 0, fp32 factor, DROPTOL 1e-3.  The
