@@ -466,6 +466,7 @@ def run_gb300(args):
     e1 = torch.cuda.Event(enable_timing=True)
     l0 = L.jdgpu_launch_count()
     iters, results = [], []
+    J.reset_stats()
     e0.record(stream)
     for _ in range(args.steps):
         r = run_solve(J, w, args, -1)
@@ -475,6 +476,7 @@ def run_gb300(args):
     barrier()
     ms = e0.elapsed_time(e1) / args.steps
     launches = L.jdgpu_launch_count() - l0
+    timed_st = J.stats(complex_=w["kind"] == "z")
     clk = clocks.stop()
     ms = max_over_ranks(ms, world, device="cuda")
     # the solver's own test (INFO = 0, all pairs returned); the final Rayleigh-Ritz
@@ -554,6 +556,8 @@ def run_gb300(args):
                        "fill": st["fill"], "nnz_l": st["nnz_l"], "levels": st["levels"],
                        "fwd_depth": st["fwd_depth"], "dense_rows": st["dense_rows"],
                        "dense_blocks": st["dense_blocks"], "matvec_per_solve": int(np.median(iters)),
+                       "precond_per_solve": timed_st["n_precond"] / args.steps,
+                       "precond_share_of_solve": timed_st["n_precond"] / args.steps * pb[0] / ms,
                        "parallelism": f"replicas x{world}", "l2": "working set > L2 (no flush needed)",
                        "eigs_min_max": [float(eigs[0]), float(eigs[-1])], "converged": ok,
                        "eigs": [float(v) for v in eigs],

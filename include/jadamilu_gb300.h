@@ -335,7 +335,10 @@ JDG_API int jdgpu_dpjd_batch(int nprob, const int* n, double* const* a, int* con
  * (1: one line per factor level and per uploaded sub-factor on stderr).
  * "plan_launch_us" (default 4) and "plan_tile_gbs" (default 5000): the cost
  * of one launch and the streaming rate the apply planner weighs when it
- * chooses which runs of sweep levels become dense tiles.
+ * chooses which runs of sweep levels become dense tiles.  "tri_cluster" (8,
+ * default, or 16): CTAs per thread-block cluster of the dense-block tile
+ * product for factors uploaded after the call (16 only where the device
+ * runs clusters of that size; otherwise 8).
  * They apply to factors computed, and solves started, after the call. */
 JDG_API void jdgpu_set_option(const char* name, double value);
 

@@ -161,8 +161,16 @@ struct Options {
   // factor a matrix shifted below or near the lower end of the spectrum)
   int large_form_isearch = 2;
   int factor_verbose = 0;
+  int tri_cluster = 8;         // CTAs per cluster of the tile product: 8, or 16 where the GPU allows it
 };
 static Options g_opt;
+
+// the tile product's cluster size for a factor uploaded now (16 only where
+// the current device runs clusters of that non-portable size)
+template <class S> static int tile_cluster() {
+  if (g_opt.tri_cluster != 16) return 8;
+  return k::tri_cluster16_ok<S, typename Arith<S>::type>() ? 16 : 8;
+}
 
 // the factor options of this library on top of the caller's droptol/condest/mem;
 // isearch: the solve's ISEARCH (2 for the factor-only and gradient entry points)
@@ -458,7 +466,9 @@ void upload_factor(const IldlcFactor<H>& F, DevFactor<S>& D, cudaStream_t st, Al
       std::vector<S> tf, tb;
       tail_inverse<H, S>(B.m, ip, ii, iv, tf, tb, nth, [](const H& v) { return StoreOf<S>::f(v); });
       B.nt = (B.m + kTile - 1) / kTile;
-      const std::vector<int> itf = make_cluster_items(B.nt, true, 8), itb = make_cluster_items(B.nt, false, 8);
+      B.tcl = tile_cluster<S>();
+      const std::vector<int> itf = make_cluster_items(B.nt, true, B.tcl),
+                             itb = make_cluster_items(B.nt, false, B.tcl);
       up_(B.tf, tf);
       up_(B.tb, tb);
       up_(B.itf, itf);
@@ -2142,6 +2152,7 @@ JDG_API void jdgpu_set_option(const char* name, double value) {
   else if (!std::strcmp(name, "large_form_isearch")) g_opt.large_form_isearch = (int)value;
   else if (!std::strcmp(name, "lookahead")) g_opt.lookahead = (int)value;
   else if (!std::strcmp(name, "factor_verbose")) g_opt.factor_verbose = (int)value;
+  else if (!std::strcmp(name, "tri_cluster")) g_opt.tri_cluster = (int)value;
 }
 
 // statistics of the last real-arithmetic solve: factor seconds, upload seconds,

@@ -409,20 +409,23 @@ template <class T> void diagsolve(long n, const double* d, const T* rhs, T* sol,
 }
 
 // ------------------------------------------------ multilevel LDL^H apply ----
-// Entries q, q + step, ... (below e) of a row, kUnr at a time: a batch's
+// Entries q, q + step, ... (below e) of a row, U at a time: a batch's
 // column indices and values are loaded together, then its gathers of y, and
 // the products are added in entry order, so the roundings are those of one
-// entry at a time while kUnr dependent load chains are in flight.
+// entry at a time while U dependent load chains are in flight.  kUnr for the
+// sweeps; the external-entry gathers of large dense blocks (rows of hundreds
+// of entries) take kUnrLong.
 constexpr int kUnr = 4;
-template <class A> struct EntBatch {
-  int c[kUnr];
-  A v[kUnr];
+constexpr int kUnrLong = 8;
+template <class A, int U> struct EntBatch {
+  int c[U];
+  A v[U];
 };
-template <bool NC, class A, class S>
-__device__ __forceinline__ void ent_load(EntBatch<A>& b, int64_t q, int64_t e, int step, const int* __restrict__ ci,
+template <bool NC, class A, int U, class S>
+__device__ __forceinline__ void ent_load(EntBatch<A, U>& b, int64_t q, int64_t e, int step, const int* __restrict__ ci,
                                          const S* __restrict__ cv) {
 #pragma unroll
-  for (int u = 0; u < kUnr; ++u) {
+  for (int u = 0; u < U; ++u) {
     const int64_t qq = q + (int64_t)u * step;
     if (qq < e) {
       b.c[u] = NC ? ld_idx_nc(ci + qq) : ci[qq];
@@ -433,12 +436,12 @@ __device__ __forceinline__ void ent_load(EntBatch<A>& b, int64_t q, int64_t e, i
     }
   }
 }
-template <class A> __device__ __forceinline__ A ent_use(const EntBatch<A>& b, const A* y, A acc) {
-  A w[kUnr];
+template <class A, int U> __device__ __forceinline__ A ent_use(const EntBatch<A, U>& b, const A* y, A acc) {
+  A w[U];
 #pragma unroll
-  for (int u = 0; u < kUnr; ++u) w[u] = b.c[u] >= 0 ? y[b.c[u]] : A(0);
+  for (int u = 0; u < U; ++u) w[u] = b.c[u] >= 0 ? y[b.c[u]] : A(0);
 #pragma unroll
-  for (int u = 0; u < kUnr; ++u)
+  for (int u = 0; u < U; ++u)
     if (b.c[u] >= 0) acc = fma_(b.v[u], w[u], acc);
   return acc;
 }
@@ -451,11 +454,11 @@ __device__ __forceinline__ void prefetch_rest(int64_t q, int64_t e, const int* _
     l2_prefetch(cv + q, sizeof(S) * (size_t)(e - q));
   }
 }
-template <bool NC, class A, class S>
+template <bool NC, int U = kUnr, class A, class S>
 __device__ __forceinline__ A ent_dot(int64_t q, int64_t e, int step, const int* __restrict__ ci,
                                      const S* __restrict__ cv, const A* y, A acc) {
-  for (; q < e; q += (int64_t)kUnr * step) {
-    EntBatch<A> b;
+  for (; q < e; q += (int64_t)U * step) {
+    EntBatch<A, U> b;
     ent_load<NC>(b, q, e, step, ci, cv);
     acc = ent_use(b, y, acc);
   }
@@ -582,7 +585,7 @@ __global__ void __launch_bounds__(WIDE_TPB) ildl_wide_kernel(int lo, int hi, con
     e = rp[s + 1];
     if (lane == 0) prefetch_rest(b + kUnr * LANES, e, ci, cv);
   }
-  EntBatch<A> first;
+  EntBatch<A, kUnr> first;
   ent_load<false>(first, b, e, LANES, ci, cv);
   pdl_wait();
   A acc = ent_use(first, (const A*)y, A(0));
@@ -603,19 +606,20 @@ __global__ void __launch_bounds__(WIDE_TPB) tail_ext_kernel(int m, int s_tail, c
                                                            const int* __restrict__ ci, const S* __restrict__ cv,
                                                            const A* y, A* out) {
   pdl_launch();
+  constexpr int U = NC ? kUnrLong : kUnr;
   const int t = blockIdx.x * (WIDE_TPB / LANES) + (threadIdx.x / LANES);
   const int lane = threadIdx.x % LANES;
   int64_t b = 0, e = 0;
   if (t < m) {
     b = rp[t] + lane;
     e = rp[t + 1];
-    if (lane == 0) prefetch_rest(b + kUnr * LANES, e, ci, cv);
+    if (lane == 0) prefetch_rest(b + U * LANES, e, ci, cv);
   }
-  EntBatch<A> first;
+  EntBatch<A, U> first;
   ent_load<NC>(first, b, e, LANES, ci, cv);
   pdl_wait();
   A acc = ent_use(first, y, A(0));
-  acc = ent_dot<NC>(b + kUnr * LANES, e, LANES, ci, cv, y, acc);
+  acc = ent_dot<NC, U>(b + U * LANES, e, LANES, ci, cv, y, acc);
   for (int o = LANES / 2; o > 0; o >>= 1) acc = acc + shfl_xor_any(acc, o);
   if (t < m && lane == 0) out[t] = y[s_tail + t] - acc;
 }
@@ -751,14 +755,15 @@ __global__ void __launch_bounds__(RUN_TPB) tail_run_kernel(int m, int s_tail, in
 constexpr int TRI_TPB = 256;  // threads per CTA of the tile kernel
 
 // Dense block product y = T x over a set of 64 x 64 tiles (column-major
-// inside a tile), with the reduction inside a thread-block cluster: the
-// TRI_CL CTAs of a cluster share one tile row and each streams a contiguous
-// chunk of its tiles (16-byte vectors of V consecutive rows of one tile
-// column per thread; per-column partial sums added in a fixed order) into a
-// 64-vector in its shared memory.  Rank 0 adds the TRI_CL vectors in rank
-// order through distributed shared memory and writes the row, so results do
-// not depend on timing.  x must not alias y.
-constexpr int TRI_CL = 8;
+// inside a tile), with the reduction inside a thread-block cluster: the CL
+// CTAs of a cluster (8, or 16 where the GPU allows that non-portable size)
+// share one tile row and each streams a contiguous chunk of its tiles
+// (16-byte vectors of V consecutive rows of one tile column per thread;
+// per-column partial sums added in a fixed order) into a 64-vector in its
+// shared memory.  Rank 0 adds the CL vectors in rank order through
+// distributed shared memory and writes the row, so results do not depend on
+// timing.  x must not alias y.  The cluster size is a launch attribute
+// (launch_tri), never left to a default.
 // 16-byte read-only load of data read once per launch (tiles): issued as
 // written, kept in its registers (no re-load at the point of use), no L1 allocation
 __device__ __forceinline__ uint4 ld_stream(const uint4* p) {
@@ -768,8 +773,8 @@ __device__ __forceinline__ uint4 ld_stream(const uint4* p) {
                : "l"(p));
   return r;
 }
-template <class S, class A>
-__global__ void __cluster_dims__(TRI_CL, 1, 1) __launch_bounds__(TRI_TPB)
+template <class S, class A, int CL>
+__global__ void __launch_bounds__(TRI_TPB)
     tri_cluster_kernel(const int4* __restrict__ items, const S* __restrict__ tiles, const A* __restrict__ x, int m,
                        A* __restrict__ y) {
   pdl_launch();
@@ -829,16 +834,64 @@ __global__ void __cluster_dims__(TRI_CL, 1, 1) __launch_bounds__(TRI_TPB)
   if (cl.block_rank() == 0 && threadIdx.x < 64) {
     A sum = A(0);
 #pragma unroll
-    for (int r = 0; r < TRI_CL; ++r) sum = sum + *cl.map_shared_rank(&mine[threadIdx.x], r);
+    for (int r = 0; r < CL; ++r) sum = sum + *cl.map_shared_rank(&mine[threadIdx.x], r);
     const int e = it.x * 64 + threadIdx.x;
     if (e < m) y[e] = sum;
   }
   cl.sync();  // the other ranks' shared memory stays alive until rank 0 has read it
 }
 
+// one launch of a cluster kernel: cl CTAs per cluster, PDL as launch_k
+template <class... Params, class... Args>
+static void launch_cl(void (*kern)(Params...), dim3 grid, dim3 block, int cl, cudaStream_t s, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute at[2];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = cl;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  at[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[1].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = g_pdl ? 2 : 1;
+  CK(cudaLaunchKernelEx(&cfg, kern, static_cast<Params>(args)...));
+}
+// items are grid-sized multiples of the cluster size (make_cluster_items)
 template <class S, class A>
-static void launch_tri(int items, const int4* it, const S* tiles, const A* x, int m, A* y, cudaStream_t s) {
-  launch_k(tri_cluster_kernel<S, A>, dim3(items), dim3(TRI_TPB), 0, s, it, tiles, x, m, y);
+static void launch_tri(int items, int cl, const int4* it, const S* tiles, const A* x, int m, A* y, cudaStream_t s) {
+  if (cl == 16) launch_cl(tri_cluster_kernel<S, A, 16>, dim3(items), dim3(TRI_TPB), 16, s, it, tiles, x, m, y);
+  else launch_cl(tri_cluster_kernel<S, A, 8>, dim3(items), dim3(TRI_TPB), 8, s, it, tiles, x, m, y);
+}
+// Whether clusters of 16 tile CTAs can run on the current device: allows the
+// non-portable size on both instantiations' kernel and asks the occupancy
+// calculator for at least one active cluster.  Called on upload, before any
+// graph capture.
+template <class S, class A> bool tri_cluster16_ok() {
+  auto kern = tri_cluster_kernel<S, A, 16>;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(16);
+  cfg.blockDim = dim3(TRI_TPB);
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = 16;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  int nc = 0;
+  if (cudaOccupancyMaxActiveClusters(&nc, kern, &cfg) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return nc > 0;
 }
 
 // raise the dynamic shared-memory limit of the tail kernel once per size
@@ -1016,7 +1069,7 @@ template <class T, class S> void ildl_apply(const DevFactor<S>& F, bool spd, con
       if (B.nt > 0) {
         // right-hand side into xb, then y_B = T xb
         ext(B.m, B.s0, B.ep, B.ei, B.ev, B.nfe, F.xb);
-        launch_tri<S, A>(B.nitf, (const int4*)B.itf, B.tf, (const A*)F.xb, B.m, yb, s);
+        launch_tri<S, A>(B.nitf, B.tcl, (const int4*)B.itf, B.tf, (const A*)F.xb, B.m, yb, s);
       } else if (B.nfe > 0) {
         ext(B.m, B.s0, B.ep, B.ei, B.ev, B.nfe, yb);
       }
@@ -1033,7 +1086,7 @@ template <class T, class S> void ildl_apply(const DevFactor<S>& F, bool spd, con
       A* yb = F.y + B.s0;
       if (B.nt > 0) {
         ext(B.m, B.s0, B.bp, B.bi, B.bv, B.nbe, F.xb);
-        launch_tri<S, A>(B.nitb, (const int4*)B.itb, B.tb, (const A*)F.xb, B.m, yb, s);
+        launch_tri<S, A>(B.nitb, B.tcl, (const int4*)B.itb, B.tb, (const A*)F.xb, B.m, yb, s);
       } else if (B.nbe > 0) {
         ext(B.m, B.s0, B.bp, B.bi, B.bv, B.nbe, yb);
       }
@@ -1096,7 +1149,8 @@ JD_INST_T(zc)
   template void ildl_apply_graph<T, S>(DevFactor<S>&, bool, const T*, T*, cudaStream_t);          \
   template void ildl_plan<S>(DevFactor<S>&, const std::vector<int64_t>&, const std::vector<int64_t>&, \
                              const std::vector<int>&);                                          \
-  template void ildl_plan_bwd0<S>(DevFactor<S>&, const std::vector<int64_t>&, const std::vector<int>&);
+  template void ildl_plan_bwd0<S>(DevFactor<S>&, const std::vector<int64_t>&, const std::vector<int>&); \
+  template bool tri_cluster16_ok<S, typename Arith<S>::type>();
 JD_INST_F(double, double)
 JD_INST_F(double, float)
 JD_INST_F(double, __nv_bfloat16)

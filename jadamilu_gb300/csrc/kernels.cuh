@@ -32,6 +32,7 @@ template <class S> struct DenseBlk {
   S* tf = nullptr; S* tb = nullptr;                            // tiles of Linv and Linv^H
   int* itf = nullptr; int* itb = nullptr;                      // work items, 4 ints each
   int nitf = 0, nitb = 0;
+  int tcl = 8;                                                 // CTAs per cluster of the tile product
   int* irf = nullptr; int* irb = nullptr;                      // items of each tile row
 };
 
@@ -138,6 +139,7 @@ template <class T, class S> void ildl_apply_graph(DevFactor<S>& F, bool spd, con
 // lanes of a warp that share one row of a given mean length in the row kernels
 int lanes_per_row(double entries_per_row);
 // split the level lists of F into wide levels and runs of narrow levels
+template <class S, class A> bool tri_cluster16_ok();
 template <class S> void ildl_plan(DevFactor<S>& F, const std::vector<int64_t>& lp_host, const std::vector<int64_t>& up_host,
                                   const std::vector<int>& brows_host);
 // make the bulk backward sweep start at level 0 (its rows may point into the tail)
