@@ -904,6 +904,21 @@ void orc_dfactor_apply(void* h, int spd, int single, const double* b, double* x)
     orc::ildl_apply(F, spd != 0, b, x, y);
   }
 }
+// The arrays of a single-L factor (test infrastructure: a test rebuilds P, L
+// and D^{-1} with scipy and checks the application against triangular
+// solves that share no code with this file).  Sizes from
+// orc_dfactor_schedule: n and nnz(L).
+void orc_dfactor_export(void* h, int* perm, long* lp, int* li, double* lx, signed char* blk, double* dinv,
+                        double* doff) {
+  auto& F = ((OrcFactorD*)h)->F;
+  std::copy(F.perm.begin(), F.perm.end(), perm);
+  for (int p = 0; p <= F.n; ++p) lp[p] = (long)F.lp[p];
+  std::copy(F.li.begin(), F.li.end(), li);
+  std::copy(F.lx.begin(), F.lx.end(), lx);
+  std::copy(F.blk.begin(), F.blk.end(), blk);
+  std::copy(F.dinv.begin(), F.dinv.end(), dinv);
+  std::copy(F.doff.begin(), F.doff.end(), doff);
+}
 void orc_dfactor_free(void* h) { delete (OrcFactorD*)h; }
 
 }  // extern "C"

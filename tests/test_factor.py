@@ -156,3 +156,49 @@ def test_coupled_form_levels_and_spd(oracle):
     Mi = np.stack([F.apply(e, spd=True) for e in np.eye(n)], 1)
     np.testing.assert_allclose(Mi, Mi.T, atol=1e-10 * np.abs(Mi).max())
     assert np.linalg.eigvalsh(0.5 * (Mi + Mi.T)).min() > 0
+
+
+@pytest.mark.parametrize("large_form", [False, True])
+def test_apply_matches_scipy_triangular_solves(oracle, large_form):
+    """The oracle's application x = P (L D L^H)^{-1} P^T b checked against
+    scipy: the factor's arrays (permutation, unit lower L, D^{-1} with 1x1
+    and 2x2 blocks) exported and applied with scipy's sparse triangular
+    solves, on an indefinite Anderson matrix with dropping (2x2 pivots,
+    several levels), plain and large-matrix factor forms."""
+    import ctypes as C
+    from scipy.sparse.linalg import spsolve_triangular
+    lib = oracle.lib()
+    p = C.c_void_p
+    lib.orc_set_coupled_min_n.argtypes = [C.c_int]
+    lib.orc_set_coupled_min_n(0 if large_form else 1 << 30)
+    try:
+        ia, ja, a = M.anderson3d(10, seed=5)
+        F = oracle.Factor(ia, ja, a, shift=0.0, droptol=1e-3)
+    finally:
+        lib.orc_set_coupled_min_n(4096)
+    assert F.ierr == 0
+    sizes = np.zeros(4, np.int64)
+    lib.orc_dfactor_schedule.argtypes = [p] * 8
+    lib.orc_dfactor_schedule(F.h, sizes.ctypes.data, None, None, None, None, None, None)
+    n, nz = int(sizes[2]), int(sizes[3])
+    perm, lp, li = np.zeros(n, np.int32), np.zeros(n + 1, np.int64), np.zeros(nz, np.int32)
+    lx, blk, dinv, doff = np.zeros(nz), np.zeros(n, np.int8), np.zeros(n), np.zeros(n)
+    lib.orc_dfactor_export.argtypes = [p] * 8
+    lib.orc_dfactor_export(F.h, *[v.ctypes.data for v in (perm, lp, li, lx, blk, dinv, doff)])
+    assert F.info()["n2x2"] > 0 and F.info()["nlevels"] >= 2
+    L = sp.csr_matrix((lx, li, lp), shape=(n, n)) + sp.eye(n, format="csr")
+    Dinv = sp.lil_matrix((n, n))
+    for s in range(n):
+        if blk[s] == 1:
+            Dinv[s, s] = dinv[s]
+        elif blk[s] == 2:
+            Dinv[s, s], Dinv[s + 1, s + 1] = dinv[s], dinv[s + 1]
+            Dinv[s, s + 1] = Dinv[s + 1, s] = doff[s]
+    b = np.random.default_rng(3).standard_normal(n)
+    y = spsolve_triangular(L.tocsr(), b[perm], lower=True, unit_diagonal=True)
+    y = Dinv.tocsr() @ y
+    y = spsolve_triangular(L.T.tocsr(), y, lower=False, unit_diagonal=True)
+    x_ref = np.empty(n)
+    x_ref[perm] = y
+    x = F.apply(b)
+    assert np.linalg.norm(x - x_ref) <= 1e-12 * np.linalg.norm(x_ref)
