@@ -9,12 +9,18 @@ import sys
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def test_reference_arm_json_line():
-    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--size", "10",
-                        "--steps", "1", "--warmup", "3"], capture_output=True, text=True, timeout=600, cwd=ROOT)
+import pytest
+
+
+@pytest.mark.parametrize("workload,size", [("anderson", 10), ("laplace", 8), ("tightbinding", 6), ("fem", 12)])
+def test_reference_arm_json_line(workload, size):
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--workload", workload,
+                        "--size", str(size), "--steps", "1", "--warmup", "3"], capture_output=True, text=True,
+                       timeout=600, cwd=ROOT)
     assert r.returncode == 0, r.stderr[-2000:]
-    lines = [ln for ln in r.stdout.strip().splitlines() if ln.startswith("{")]
-    assert len(lines) == 1
+    # standard output carries the result line alone (the solver's own messages go to stderr)
+    lines = r.stdout.strip().splitlines()
+    assert len(lines) == 1 and lines[0].startswith("{"), r.stdout[-2000:]
     d = json.loads(lines[0])
     for k in ("impl", "metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
               "scaling", "vs_baseline", "dtype", "data", "config", "e2e", "cpu_baseline"):
