@@ -15,8 +15,14 @@
 // project's host factorisation (jadamilu_gb300/csrc/ildlc.hpp); the oracle
 // applies it with sequential triangular solves.
 //
+// Pinned by the reference's own results (the user guide's sample outputs,
+// tests/golden/userguide_kats.json), by eigenvalues of solvers that share no
+// code with it (ARPACK Lanczos and shift-and-invert fixtures under
+// tests/golden/), and its factor application by scipy triangular solves
+// (tests/test_factor.py).
+//
 // Loaded by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg
-// only.  The GPU library never links or calls it.
+// and reference arm only.  The GPU library never links or calls it.
 #include <chrono>
 #include <complex>
 #include <cstdint>
