@@ -63,12 +63,13 @@ def test_ildl_apply_bf16_is_a_preconditioner(gpu, oracle):
     assert np.linalg.norm(xb - xo) / np.linalg.norm(xo) < 5e-2
 
 
-@pytest.mark.parametrize("variant", ["levels", "small_dense", "dense"])
+@pytest.mark.parametrize("variant", ["levels", "small_dense", "dense", "dense_cluster16"])
 @pytest.mark.parametrize("precision,tol", [(0, 1e-11), (1, 2e-5)])
 def test_ildl_apply_tail_variants_match_oracle(gpu, oracle, variant, precision, tol):
     """The deepest levels solved level by level in one CTA, with the explicit
     inverse of a block capped at 100 rows, and with the block the cost model
-    picks give the oracle's substitution result."""
+    picks (tile products in clusters of 8 CTAs, or of 16 where the device
+    allows) give the oracle's substitution result."""
     ia, ja, a = M.anderson3d(20, seed=3)
     n = len(ia) - 1
     F = oracle.Factor(ia, ja, a, shift=0.0, droptol=1e-3, mem=0)
@@ -78,10 +79,13 @@ def test_ildl_apply_tail_variants_match_oracle(gpu, oracle, variant, precision, 
             gpu.set_option("dense_tail", 0)
         elif variant == "small_dense":
             gpu.set_option("dense_max", 100)
+        elif variant == "dense_cluster16":
+            gpu.set_option("tri_cluster", 16)
         Xg, info = gpu.ildl_apply((a, ja, ia), B, shift=0.0, droptol=1e-3, spd=False, precision=precision)
     finally:
         gpu.set_option("dense_tail", 1)
         gpu.set_option("dense_max", 32768)
+        gpu.set_option("tri_cluster", 8)
     for r in range(2):
         # fp32 results are compared with the exact (fp64) application, within a
         # small multiple of the oracle's own fp32 substitution error
