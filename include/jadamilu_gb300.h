@@ -338,7 +338,9 @@ JDG_API int jdgpu_dpjd_batch(int nprob, const int* n, double* const* a, int* con
  * chooses which runs of sweep levels become dense tiles.  "tri_cluster" (8,
  * default, or 16): CTAs per thread-block cluster of the dense-block tile
  * product for factors uploaded after the call (16 only where the device
- * runs clusters of that size; otherwise 8).
+ * runs clusters of that size; otherwise 8).  "dense_min_rows" (default
+ * 8192): a factor level at least a quarter full is eliminated densely from
+ * this many rows on.
  * They apply to factors computed, and solves started, after the call. */
 JDG_API void jdgpu_set_option(const char* name, double value);
 

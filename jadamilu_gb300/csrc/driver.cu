@@ -162,6 +162,7 @@ struct Options {
   int large_form_isearch = 2;
   int factor_verbose = 0;
   int tri_cluster = 8;         // CTAs per cluster of the tile product: 8, or 16 where the GPU allows it
+  int dense_min_rows = -1;     // IldlcParams::dense_min_rows (negative: its default)
 };
 static Options g_opt;
 
@@ -179,6 +180,7 @@ static void factor_options(IldlcParams& p, int n, int isearch = 2) {
   p.droptol_schur = g_opt.drop_schur;
   p.matching = g_opt.matching;
   p.verbose = g_opt.factor_verbose;
+  if (g_opt.dense_min_rows >= 0) p.dense_min_rows = g_opt.dense_min_rows;
   if (n >= g_opt.coupled_min_n && isearch >= g_opt.large_form_isearch) {
     p.coupling = g_opt.coupling;
     p.drop_rule = g_opt.drop_rule;
@@ -2153,6 +2155,7 @@ JDG_API void jdgpu_set_option(const char* name, double value) {
   else if (!std::strcmp(name, "lookahead")) g_opt.lookahead = (int)value;
   else if (!std::strcmp(name, "factor_verbose")) g_opt.factor_verbose = (int)value;
   else if (!std::strcmp(name, "tri_cluster")) g_opt.tri_cluster = (int)value;
+  else if (!std::strcmp(name, "dense_min_rows")) g_opt.dense_min_rows = (int)value;
 }
 
 // statistics of the last real-arithmetic solve: factor seconds, upload seconds,
