@@ -32,3 +32,23 @@ def test_reference_arm_json_line(workload, size):
     cb = d["cpu_baseline"]
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["sample"] and cb["value"] == d["value"]
     assert "workload" in d["config"]
+
+
+@pytest.mark.parametrize("workload,size,neig", [("tightbinding", 8, 8), ("fem", 16, 6)])
+def test_cpu_baseline_with_the_oracles_own_factor(workload, size, neig):
+    """The CPU-baseline leg of the complex and generalized workloads (whose
+    factors are not exported): the oracle factors the same matrix itself and
+    its per-MATVEC time is scaled to the GPU solve's MATVEC count."""
+    sys.path.insert(0, ROOT)
+    import bench
+    old = sys.argv
+    try:
+        sys.argv = ["bench.py", "--workload", workload, "--size", str(size), "--neig", str(neig),
+                    "--cpu-seconds", "1"]
+        args = bench.parse()
+    finally:
+        sys.argv = old
+    w = bench.make_workload(args)
+    cb = bench.cpu_baseline_own_factor(args, w, 300)
+    assert cb["kind"] == "port" and cb["cores"] == 1 and cb["unit"] == "s"
+    assert cb["value"] > 0 and "MATVECs" in cb["sample"]
